@@ -1,0 +1,425 @@
+"""Benchmark of the headline workload: full development of 5760x3240 RGGB
+12-bit frames -- VST + NLM 1.0 (7x7 search, 3x3 patch) + RCD + matrix to
+ACES AP1 float32 RGBA (with the ACES 1.3 gamut compression) + the AWB
+histogram -- on one GB300 per process.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fused|plain|reference]
+                    [--storage fp32|fp16]
+
+One JSON line on rank 0. A step develops one frame through
+craw_pipeline_record() (libcraw.so). ``value`` is frames/s with the mosaic
+resident in device memory, from CUDA events around every step on the
+recording stream, L2 flushed (a 256 MB write) between steps; ``e2e`` is
+the same metric through the same call with the mosaic copied in from and
+the RGBA32F frame copied out to pinned host memory inside the timed
+region. ``roofline`` is the dominant kernel's (the denoise) HBM view and
+``roofline_fp32`` its FP32-pipe view; ``cpu_baseline`` is the CPU oracle
+(a port of the reference's lib/ref) on the host cores.
+
+Under torchrun every rank develops its own frames (replicas: the path has
+no exchange step); ``value`` is all ranks' frames over the slowest rank's
+time.
+
+``--impl reference`` times the reference's CPU implementation of the path
+(the oracle port of lib/ref; the reference's own compiled code is only
+available where its source tree is) with all host threads, on the same
+config, and prints the same kind of line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+import numpy as np  # noqa: E402
+
+METRIC = "5760x3240 frames/s full develop; p50/p99 frame latency at <=1e-3 rel err"
+WORKLOAD = "5760x3240 RGGB 12-bit: VST + NLM 1.0 + RCD + ACES AP1 (RGC) float32 + AWB histogram"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="fused", choices=["fused", "plain", "reference"])
+    ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16"])
+    ap.add_argument("--no-extras", action="store_true", help="skip the plain/fp16/cpu side runs")
+    ap.add_argument("--width", type=int, default=5760)
+    ap.add_argument("--height", type=int, default=3240)
+    return ap.parse_args()
+
+
+# ------------------------------------------------------------------ clocks
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], 0.0, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = max(mx, float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ----------------------------------------------------------------- helpers
+
+def peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": d.get("hbm_gbs", 6800.0), "src": "measured"}
+    return {"hbm_gbs": 6800.0, "src": "fallback"}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0
+    import torch.distributed as dist
+    rank, local = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
+    import torch
+    torch.cuda.set_device(local)
+    dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return rank, ws, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ------------------------------------------------------------- CPU baseline
+
+def cpu_oracle_fps(frame: np.ndarray, params, fp, rows_frac: float = 0.25) -> dict:
+    """The CPU oracle (float restatement of the reference's lib/ref) on
+    `rows_frac` of a frame, split into one strip per host thread, each strip
+    developed as a frame of its own: frames/s = rows_frac / wall time."""
+    sys.path.insert(0, str(ROOT / "tests"))
+    from oracle import Oracle
+    import libcraw_gb300 as L
+
+    orc = Oracle()
+    cores = os.cpu_count() or 1
+    h, w = frame.shape
+    rows = max(16, int(h * rows_frac) // cores // 2 * 2)
+    strips = [np.ascontiguousarray(frame[i * rows:(i + 1) * rows]) for i in range(cores)]
+    pps = [L.pipeline_params(w, rows, debayer=params.debayer, out_space=params.out_space,
+                             flags=params.flags, out_format=L.FORMAT_RGBA32F) for _ in strips]
+    outs = [None] * cores
+
+    def work(i):
+        outs[i] = orc.process(strips[i], pps[i], fp, "f32")
+
+    threads = [threading.Thread(target=work, args=(i,)) for i in range(cores)]
+    t0 = time.perf_counter()
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    dt = time.perf_counter() - t0
+    done = rows * cores / h
+    return {"value": done / dt, "unit": "frames/s", "cores": cores, "kind": "port",
+            "sample": f"{cores} strips of {w}x{rows} ({done:.3f} of a frame) through the float "
+                      f"oracle (lib/ref restated), one strip per host thread, {dt:.2f} s wall"}
+
+
+def run_reference(args):
+    # Rank 0 alone runs the CPU baseline; the other ranks have no work.
+    if int(os.environ.get("RANK", "0")) != 0:
+        return
+    ws = 1
+    import libcraw_gb300 as L
+    from libcraw_gb300 import build as B
+    from libcraw_gb300 import workloads as W
+    B.build()
+    c = W.config(2, args.width, args.height)
+    frame = c.frame()
+    prof = W.make_profile()
+    pp = L.pipeline_params(c.width, c.height, debayer=c.debayer, out_space=c.out_space, flags=c.flags,
+                           out_format=L.FORMAT_RGBA32F)
+    fp = L.frame_params(prof, **c.frame_kwargs())
+    frac = 0.125
+    for _ in range(args.warmup):
+        cpu_oracle_fps(frame, pp, fp, frac)
+    times = []
+    last = None
+    for _ in range(args.steps):
+        last = cpu_oracle_fps(frame, pp, fp, frac)
+        times.append(frac / last["value"])
+    total = sum(times)
+    value = args.steps * frac / total
+    lat = sorted(t / frac * 1000 for t in times)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "frames/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total / args.steps * 1000, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, config 2)",
+        "config": {"workload": WORKLOAD, "width": c.width, "height": c.height},
+        "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
+        "cpu_baseline": {**last, "value": value},
+        "e2e": {"value": value, "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    barrier(ws)
+
+
+# --------------------------------------------------------------- GPU arm
+
+def run_gpu(args):
+    import torch
+
+    rank, ws, local = dist_init()
+    import libcraw_gb300 as L
+    from libcraw_gb300 import build as B
+    from libcraw_gb300 import workloads as W
+    if rank == 0 or ws == 1:
+        B.build()
+    barrier(ws)
+    torch.cuda.set_device(local)
+    dev = torch.cuda.current_device()
+    props = torch.cuda.get_device_properties(dev)
+
+    c = W.config(2, args.width, args.height)
+    w, h = c.width, c.height
+    prof = W.make_profile()
+    fp = L.frame_params(prof, **c.frame_kwargs())
+    storage = L.STORAGE_FP16 if args.storage == "fp16" else L.STORAGE_FP32
+    impl = L.IMPL_PLAIN if args.impl == "plain" else L.IMPL_FUSED
+
+    # Four distinct frames in rotation (different seeds), 16-byte rows.
+    nfr = 4
+    host_frames = [W.synth_frame(w, h, c.seed + 7919 * rank + i, rects=c.rects, zone_plates=c.zone_plates,
+                                 noise_a_dn=c.noise_a_dn, noise_b_dn=c.noise_b_dn) for i in range(nfr)]
+    dev_frames = [torch.from_numpy(f.view(np.int16)).cuda() for f in host_frames]
+    srcs = [L.Image(t.data_ptr(), w * 2, L.FORMAT_R16_UNORM, w, h) for t in dev_frames]
+    out = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    dst = L.Image(out.data_ptr(), w * 16, L.FORMAT_RGBA32F, w, h)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+
+    ctx = L.Context(dev)
+    stream = torch.cuda.Stream()
+    sptr = stream.cuda_stream
+
+    def make_pipe(impl_, storage_, profile=True):
+        flags = c.flags | (L.FLAG_PROFILE if profile else 0)
+        return L.Pipeline(ctx, L.pipeline_params(w, h, debayer=c.debayer, out_space=c.out_space,
+                                                 flags=flags, out_format=L.FORMAT_RGBA32F,
+                                                 storage=storage_, impl=impl_, nb_awb_slots=2))
+
+    def timed(pipe, steps, warmup, collect=True):
+        with torch.cuda.stream(stream):
+            for i in range(warmup):
+                pipe.record(sptr, srcs[i % nfr], dst, fp)
+            torch.cuda.synchronize()
+            barrier(ws)
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(steps)]
+            stage: dict[str, list[float]] = {}
+            t0 = time.perf_counter()
+            for i in range(steps):
+                flush.zero_()
+                evs[i][0].record(stream)
+                pipe.record(sptr, srcs[i % nfr], dst, fp)
+                evs[i][1].record(stream)
+                if collect:
+                    evs[i][1].synchronize()
+                    for name, cnt, ms in pipe.stage_times():
+                        stage.setdefault(name, []).append(ms)
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - t0
+        barrier(ws)
+        ms = [a.elapsed_time(b) for a, b in evs]
+        return ms, stage, wall
+
+    pipe = make_pipe(impl, storage)
+    with ClockSampler(dev) as clk:
+        ms, stage, wall = timed(pipe, args.steps, max(3, args.warmup))
+    total_s = sum(ms) / 1000.0
+    slowest = max_over_ranks(total_s, ws)
+    value = ws * args.steps / slowest
+    lat = sorted(ms)
+    hist = pipe.awb_histogram()
+
+    # The roofline of the dominant kernel, from its own events in the timed region.
+    dom = max(stage, key=lambda k: sum(stage[k])) if stage else None
+    dom_ms = statistics.mean(stage[dom]) if dom else None
+    n_px = w * h
+    pk = peaks()
+    roof = roof32 = None
+    if dom:
+        # Algorithmic bytes per launch of the denoise: mosaic in (2 B/px), denoised
+        # mosaic out (2 B/px); of the develop: mosaic in (2) + RGBA32F out (16)
+        # + AWB records (8 per 64 px).
+        bpp = {"denoise_nlm": 4.0, "develop": 18.0 + 8.0 / 64, "plain_denoise": 4.0,
+               "plain_develop": 18.0}.get(dom, 4.0)
+        achieved = bpp * n_px / (dom_ms / 1000.0) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
+                "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                "peak_src": pk["src"], "bytes_per_px": bpp, "ms_per_launch": dom_ms}
+        if dom.endswith("denoise_nlm") or dom == "plain_denoise":
+            clk_s = clk.summary()
+            mhz = clk_s["sm_mhz"] or 2070.0
+            peak_lane_ops = props.multi_processor_count * 128 * mhz * 1e6 / 1e12
+            ops = n_px * 49 * 13 / (dom_ms / 1000.0) / 1e12
+            roof32 = {"bound": "fp32", "achieved": ops, "peak": peak_lane_ops, "unit": "Tlane-op/s",
+                      "frac": ops / peak_lane_ops,
+                      "model": "N*49*13 FP32 lane-ops per frame (7x7 search, 13 ops an offset); "
+                               "peak = SMs x 128 FP32 lanes x median SM clock"}
+
+    # End to end through the same call: pinned host mosaic in, RGBA32F out.
+    pinned_in = [torch.from_numpy(f.view(np.int16)).pin_memory() for f in host_frames]
+    pinned_out = torch.empty((h, w, 4), dtype=torch.float32).pin_memory()
+    dev_in = torch.empty((h, w), dtype=torch.int16, device="cuda")
+    src_e = L.Image(dev_in.data_ptr(), w * 2, L.FORMAT_R16_UNORM, w, h)
+    e2e_pipe = make_pipe(impl, storage, profile=False)
+    with torch.cuda.stream(stream):
+        for i in range(3):
+            dev_in.copy_(pinned_in[i % nfr], non_blocking=True)
+            e2e_pipe.record(sptr, src_e, dst, fp)
+            pinned_out.copy_(out, non_blocking=True)
+        torch.cuda.synchronize()
+        barrier(ws)
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            dev_in.copy_(pinned_in[i % nfr], non_blocking=True)
+            e2e_pipe.record(sptr, src_e, dst, fp)
+            pinned_out.copy_(out, non_blocking=True)
+        torch.cuda.synchronize()
+        e2e_s = time.perf_counter() - t0
+    e2e_s = max_over_ranks(e2e_s, ws)
+    e2e = {"value": ws * args.steps / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": w * h * 2,
+           "d2h_bytes_per_step": w * h * 16,
+           "how": "per step: H2D of the mosaic from pinned memory, craw_pipeline_record, D2H of "
+                  "the RGBA32F frame to pinned memory, one stream, wall clock"}
+
+    extras = {}
+    if not args.no_extras and rank == 0:
+        for name, (im, st) in {"plain_fp32": (L.IMPL_PLAIN, L.STORAGE_FP32),
+                               "fused_fp16": (L.IMPL_FUSED, L.STORAGE_FP16),
+                               "fused_fp32": (L.IMPL_FUSED, L.STORAGE_FP32)}.items():
+            if im == impl and st == storage:
+                continue
+            with make_pipe(im, st, profile=False) as p2:
+                m2, _, _ = timed(p2, max(5, args.steps // 3), 3, collect=False)
+            extras[name] = {"fps": 1000.0 / statistics.mean(m2), "ms_per_frame": statistics.mean(m2)}
+        base = extras.get("plain_fp32", {}).get("fps")
+        if base:
+            extras["speedup_vs_plain_fp32"] = (args.steps / total_s) / base
+
+    cpu = None
+    if rank == 0 and not args.no_extras:
+        cpu = cpu_oracle_fps(host_frames[0], L.pipeline_params(w, h, debayer=c.debayer, out_space=c.out_space,
+                                                              flags=c.flags), fp, 0.125)
+
+    if rank == 0:
+        clk_s = clk.summary()
+        line = {
+            "metric": METRIC, "value": value, "unit": "frames/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": max(3, args.warmup), "ms_per_step": sum(ms) / len(ms),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic: seeded generator (gradient + 256 rectangles + 4 zone plates, "
+                    "Poisson-Gaussian noise a=4 DN, b=40 DN^2), 4 frames in rotation",
+            "config": {"workload": WORKLOAD, "width": w, "height": h, "impl": args.impl,
+                       "storage": args.storage, "l2": "flushed between steps (256 MB write)",
+                       "parallelism": f"replicas x{ws}"},
+            "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                           "max": lat[-1]},
+            "stage_ms": {k: statistics.mean(v) for k, v in stage.items()},
+            "roofline": roof, "roofline_fp32": roof32,
+            "e2e": e2e,
+            # Our kernels per step: fused = denoise, develop, awb_reduce; plain =
+            # vst + nlm, prep + 8 RCD sweeps + awb + colour.
+            "gpu_launches": args.steps * (3 if impl == L.IMPL_FUSED else 13),
+            "clocks": {k: clk_s[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
+            "awb_samples": int(hist.count.sum()),
+            "wall_s_timed": wall,
+            "extras": extras,
+            "cpu_baseline": cpu,
+            "device": props.name,
+        }
+        print(json.dumps(line), flush=True)
+    pipe.close()
+    e2e_pipe.close()
+    ctx.close()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

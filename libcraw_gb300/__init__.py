@@ -1,0 +1,475 @@
+"""craw-gb300: libcraw's frame-development path on one NVIDIA GB300.
+
+This module is the Python host mirror of the ``craw_*`` C ABI
+(``include/craw/*.h``) that ``_lib/libcraw.so`` exports: the same structs
+(byte compatible, checked at import), the same functions, the same
+negative-errno error behaviour (raised here as :class:`CrawError`). It is
+plumbing over the C library; every frame goes through the sm_103a kernels
+in ``libcraw.so`` and there is no other implementation to fall back to.
+
+The reference's entry points and what replaces them (reference files):
+
+====================================  =====================================
+reference (include/craw/*.h)          here
+====================================  =====================================
+craw_context_create(VkDevice ...)     :class:`Context` (CUDA device ordinal)
+craw_pipeline_create                  :class:`Pipeline`
+craw_pipeline_record(VkCommandBuffer) :meth:`Pipeline.record` (cudaStream_t)
+craw_pipeline_get_awb_histogram[_n]   :meth:`Pipeline.awb_histogram`
+craw_pipeline_get_stage_times[_n]     :meth:`Pipeline.stage_times`
+craw_profile_eval / colorspace ...    module functions of the same names
+====================================  =====================================
+"""
+from __future__ import annotations
+
+import ctypes as C
+import errno as _errno
+import os
+from pathlib import Path
+
+import numpy as np
+
+_HERE = Path(__file__).resolve().parent
+LIB_DIR = _HERE / "_lib"
+
+# --------------------------------------------------------------- constants
+
+CFA_RGGB = 0
+DEBAYER_BILINEAR, DEBAYER_MHC, DEBAYER_RCD = 0, 1, 2
+(CS_XYZ_D65, CS_BT709, CS_BT2020, CS_P3D65, CS_V_GAMUT, CS_ACES_AP0,
+ CS_ACES_AP1) = range(7)
+FORMAT_R16_UNORM, FORMAT_RGBA16F, FORMAT_RGBA32F = 70, 97, 109
+WB_AS_SHOT, WB_REBALANCE = 0, 1
+STORAGE_FP32, STORAGE_FP16 = 0, 1
+IMPL_FUSED, IMPL_PLAIN = 0, 1
+
+FLAG_AWB_HISTOGRAM = 1 << 0
+FLAG_DENOISE = 1 << 1
+FLAG_LENS = 1 << 2
+FLAG_FALSE_COLOR = 1 << 3
+FLAG_CHROMA_DENOISE = 1 << 4
+FLAG_HIGHLIGHT_RECONSTRUCTION = 1 << 5
+FLAG_DEFRINGE = 1 << 6
+FLAG_TEMPORAL_DENOISE = 1 << 7
+FLAG_SHARPEN = 1 << 8
+FLAG_PROFILE = 1 << 9
+FLAG_KEEP_INTERMEDIATE = 1 << 16
+
+FRAME_CLAMP_NEGATIVE = 1 << 0
+FRAME_NO_GAMUT_COMPRESSION = 1 << 2
+FRAME_TEMPORAL_RESET = 1 << 4
+
+AWB_BINS = 128
+PROFILE_SLOTS = 4
+
+# ----------------------------------------------------------------- structs
+
+
+class WbKnot(C.Structure):
+    _fields_ = [("cct", C.c_float), ("wb", C.c_float * 3)]
+
+
+class MatrixKnot(C.Structure):
+    _fields_ = [("cct", C.c_float), ("m", (C.c_float * 3) * 3)]
+
+
+class NoiseKnot(C.Structure):
+    _fields_ = [("iso", C.c_float), ("a", C.c_float), ("b", C.c_float)]
+
+
+class NoiseModel(C.Structure):
+    _fields_ = [("a", C.c_float), ("b", C.c_float)]
+
+
+class Illuminant(C.Structure):
+    _fields_ = [("cct", C.c_float), ("tint", C.c_float)]
+
+
+class Profile(C.Structure):
+    _fields_ = [
+        ("cfa", C.c_int),
+        ("black_level", C.c_float * 4),
+        ("white_level", C.c_float * 4),
+        ("as_shot_wb", C.c_float * 3),
+        ("as_shot_matrix", (C.c_float * 3) * 3),
+        ("as_shot_cct", C.c_float),
+        ("gain", C.c_float),
+        ("as_shot_ei", C.c_float),
+        ("exposure_index", C.c_float),
+        ("wb_knots", WbKnot * 16),
+        ("nb_wb_knots", C.c_uint32),
+        ("matrix_knots", MatrixKnot * 16),
+        ("nb_matrix_knots", C.c_uint32),
+        ("name", C.c_char * 64),
+        ("noise_knots", NoiseKnot * 16),
+        ("nb_noise_knots", C.c_uint32),
+    ]
+
+
+class ColorParams(C.Structure):
+    _fields_ = [("wb", C.c_float * 3), ("cam_to_xyz", (C.c_float * 3) * 3), ("gain", C.c_float)]
+
+
+class LensCorrection(C.Structure):
+    _fields_ = [("k", (C.c_float * 4) * 3), ("centre", C.c_float * 2), ("valid", C.c_bool),
+                ("reserved", C.c_uint8 * 7)]
+
+
+class FrameParams(C.Structure):
+    _fields_ = [
+        ("profile", C.POINTER(Profile)),
+        ("wb_mode", C.c_int),
+        ("illuminant", Illuminant),
+        ("exposure_stops", C.c_float),
+        ("flags", C.c_uint32),
+        ("out_space", C.c_int),
+        ("out_space_set", C.c_bool),
+        ("denoise_strength", C.c_float),
+        ("noise_override", NoiseModel),
+        ("false_color_passes", C.c_uint32),
+        ("denoise_chroma_strength", C.c_float),
+        ("lens", LensCorrection),
+        ("defringe_strength", C.c_float),
+        ("denoise_temporal_strength", C.c_float),
+        ("denoise_temporal_replay", C.c_bool),
+        ("sharpen_radius", C.c_float),
+        ("sharpen_iterations", C.c_uint32),
+        ("sharpen_contrast", C.c_float),
+        ("rotation", C.c_float),
+        ("padding", C.c_uint8 * 112),
+    ]
+
+
+class PipelineParams(C.Structure):
+    _fields_ = [
+        ("width", C.c_uint32), ("height", C.c_uint32), ("cfa", C.c_int), ("debayer", C.c_int),
+        ("out_space", C.c_int), ("out_format", C.c_int), ("flags", C.c_uint32),
+        ("nb_awb_slots", C.c_uint32), ("storage", C.c_int), ("impl", C.c_int),
+        ("padding", C.c_uint8 * 216),
+    ]
+
+
+class CudaInitParams(C.Structure):
+    _fields_ = [("device", C.c_int), ("mem_pool", C.c_void_p), ("padding", C.c_uint8 * 48)]
+
+
+LOG_CB = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_char_p, C.c_void_p)
+
+
+class ContextOptions(C.Structure):
+    _fields_ = [("log_opaque", C.c_void_p), ("log_cb", C.c_void_p), ("log_level", C.c_int),
+                ("padding", C.c_uint8 * 1004)]
+
+
+class Image(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("pitch", C.c_size_t), ("format", C.c_int),
+                ("width", C.c_uint32), ("height", C.c_uint32)]
+
+
+class AwbHistogramC(C.Structure):
+    _fields_ = [("bins", C.c_uint32), ("log_min", C.c_float), ("log_max", C.c_float),
+                ("count", C.POINTER(C.c_uint32)), ("weight", C.POINTER(C.c_uint32)),
+                ("weight_bright", C.POINTER(C.c_uint32))]
+
+
+class StageTime(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("count", C.c_uint32), ("ms", C.c_double)]
+
+
+for _s, _n in ((Profile, 1264), (FrameParams, 264), (PipelineParams, 256), (CudaInitParams, 64),
+               (ContextOptions, 1024), (LensCorrection, 64)):
+    assert C.sizeof(_s) == _n, (_s.__name__, C.sizeof(_s), _n)
+
+# ----------------------------------------------------------------- library
+
+#: Every symbol the C ABI exports (include/craw/*.h).
+EXPORTS = (
+    "craw_version_int", "craw_log", "craw_context_create", "craw_context_free",
+    "craw_cuda_check_device", "craw_debug_fail_alloc",
+    "craw_pipeline_params_init", "craw_frame_params_init", "craw_pipeline_create",
+    "craw_pipeline_free", "craw_pipeline_record", "craw_pipeline_get_awb_histogram",
+    "craw_pipeline_get_awb_histogram_n", "craw_pipeline_get_stage_times",
+    "craw_pipeline_get_stage_times_n", "craw_pipeline_get_intermediate",
+    "craw_pipeline_get_temporal_state",
+    "craw_profile_init", "craw_profile_validate", "craw_profile_eval",
+    "craw_profile_noise_eval", "craw_noise_model_eval", "craw_colorspace_from_xyz_d65",
+    "craw_colorspace_to_xyz_d65", "craw_planckian_xy", "craw_bradford_adaptation",
+    "craw_awb_histogram_from_rgb",
+)
+
+
+class CrawError(RuntimeError):
+    """A negative errno returned by the C library."""
+
+    def __init__(self, code: int, what: str = ""):
+        self.code = code
+        self.errno = -code
+        name = _errno.errorcode.get(-code, str(-code))
+        super().__init__(f"{what or 'craw'} failed: {name} ({code})")
+
+
+def _check(ret: int, what: str) -> int:
+    if ret < 0:
+        raise CrawError(ret, what)
+    return ret
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    """Loads ``_lib/libcraw.so`` (built by ``libcraw_gb300.build``); raises if
+    it is missing: there is no fallback implementation."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = LIB_DIR / "libcraw.so"
+    if not path.exists():
+        raise ImportError(f"{path} is missing: run libcraw_gb300.build.build() first")
+    L = C.CDLL(str(path))
+    vp, u32, i32, f32 = C.c_void_p, C.c_uint32, C.c_int, C.c_float
+    sig = {
+        "craw_version_int": (u32, []),
+        "craw_context_create": (i32, [C.POINTER(vp), C.POINTER(CudaInitParams), C.POINTER(ContextOptions)]),
+        "craw_context_free": (None, [C.POINTER(vp)]),
+        "craw_cuda_check_device": (i32, [i32, C.POINTER(C.c_char_p)]),
+        "craw_debug_fail_alloc": (None, [i32]),
+        "craw_pipeline_params_init": (None, [C.POINTER(PipelineParams)]),
+        "craw_frame_params_init": (None, [C.POINTER(FrameParams)]),
+        "craw_pipeline_create": (i32, [vp, C.POINTER(PipelineParams), C.POINTER(vp)]),
+        "craw_pipeline_free": (None, [C.POINTER(vp)]),
+        "craw_pipeline_record": (i32, [vp, vp, C.POINTER(Image), C.POINTER(Image), C.POINTER(FrameParams)]),
+        "craw_pipeline_get_awb_histogram_n": (i32, [vp, u32, C.POINTER(AwbHistogramC)]),
+        "craw_pipeline_get_stage_times_n": (i32, [vp, u32, C.POINTER(StageTime), u32]),
+        "craw_pipeline_get_intermediate": (i32, [vp, C.POINTER(Image), C.POINTER(Image)]),
+        "craw_pipeline_get_temporal_state": (i32, [vp, C.POINTER(Image), C.POINTER(Image)]),
+        "craw_profile_init": (None, [C.POINTER(Profile)]),
+        "craw_profile_validate": (i32, [C.POINTER(Profile)]),
+        "craw_profile_eval": (i32, [C.POINTER(Profile), i32, C.POINTER(Illuminant), C.POINTER(ColorParams)]),
+        "craw_profile_noise_eval": (i32, [C.POINTER(Profile), f32, C.POINTER(NoiseModel)]),
+        "craw_noise_model_eval": (i32, [C.POINTER(NoiseKnot), u32, f32, C.POINTER(NoiseModel)]),
+        "craw_colorspace_from_xyz_d65": (i32, [i32, C.POINTER(C.c_float * 9)]),
+        "craw_colorspace_to_xyz_d65": (i32, [i32, C.POINTER(C.c_float * 9)]),
+        "craw_planckian_xy": (i32, [f32, C.POINTER(C.c_float * 2)]),
+        "craw_bradford_adaptation": (i32, [C.POINTER(C.c_float * 2), C.POINTER(C.c_float * 2),
+                                           C.POINTER(C.c_float * 9)]),
+        "craw_awb_histogram_from_rgb": (i32, [vp, u32, u32, C.c_size_t, i32, C.POINTER(C.c_float * 3),
+                                              vp, vp, vp]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = L
+    return L
+
+
+def version() -> tuple[int, int, int]:
+    v = lib().craw_version_int()
+    return (v >> 16) & 0xFF, (v >> 8) & 0xFF, v & 0xFF
+
+
+# ------------------------------------------------------------ host helpers
+
+def profile_init() -> Profile:
+    p = Profile()
+    lib().craw_profile_init(C.byref(p))
+    return p
+
+
+def profile_validate(p: Profile) -> None:
+    _check(lib().craw_profile_validate(C.byref(p)), "craw_profile_validate")
+
+
+def profile_eval(p: Profile, mode: int = WB_AS_SHOT, illum: Illuminant | None = None) -> ColorParams:
+    out = ColorParams()
+    _check(lib().craw_profile_eval(C.byref(p), mode, C.byref(illum) if illum else None, C.byref(out)),
+           "craw_profile_eval")
+    return out
+
+
+def profile_noise_eval(p: Profile, iso: float = 0.0) -> NoiseModel:
+    out = NoiseModel()
+    _check(lib().craw_profile_noise_eval(C.byref(p), iso, C.byref(out)), "craw_profile_noise_eval")
+    return out
+
+
+def noise_model_eval(knots: list[tuple[float, float, float]], iso: float) -> NoiseModel:
+    arr = (NoiseKnot * max(1, len(knots)))(*[NoiseKnot(*k) for k in knots])
+    out = NoiseModel()
+    _check(lib().craw_noise_model_eval(arr, len(knots), iso, C.byref(out)), "craw_noise_model_eval")
+    return out
+
+
+def colorspace_from_xyz_d65(cs: int) -> np.ndarray:
+    m = (C.c_float * 9)()
+    _check(lib().craw_colorspace_from_xyz_d65(cs, C.byref(m)), "craw_colorspace_from_xyz_d65")
+    return np.frombuffer(m, dtype=np.float32).reshape(3, 3).copy()
+
+
+def colorspace_to_xyz_d65(cs: int) -> np.ndarray:
+    m = (C.c_float * 9)()
+    _check(lib().craw_colorspace_to_xyz_d65(cs, C.byref(m)), "craw_colorspace_to_xyz_d65")
+    return np.frombuffer(m, dtype=np.float32).reshape(3, 3).copy()
+
+
+def planckian_xy(cct: float) -> tuple[float, float]:
+    xy = (C.c_float * 2)()
+    _check(lib().craw_planckian_xy(cct, C.byref(xy)), "craw_planckian_xy")
+    return xy[0], xy[1]
+
+
+def bradford_adaptation(src, dst) -> np.ndarray:
+    s, d, m = (C.c_float * 2)(*src), (C.c_float * 2)(*dst), (C.c_float * 9)()
+    _check(lib().craw_bradford_adaptation(C.byref(s), C.byref(d), C.byref(m)), "craw_bradford_adaptation")
+    return np.frombuffer(m, dtype=np.float32).reshape(3, 3).copy()
+
+
+def awb_histogram_from_rgb(rgb: np.ndarray, wb_applied) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+    """CPU builder over an (h, w, 3|4) float32 array."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.float32)
+    h, w, ch = rgb.shape
+    out = [np.zeros(AWB_BINS * AWB_BINS, np.uint32) for _ in range(3)]
+    wb = (C.c_float * 3)(*wb_applied)
+    _check(lib().craw_awb_histogram_from_rgb(rgb.ctypes.data, w, h, w * ch, ch, C.byref(wb),
+                                             *[o.ctypes.data for o in out]),
+           "craw_awb_histogram_from_rgb")
+    return tuple(o.reshape(AWB_BINS, AWB_BINS) for o in out)
+
+
+def pipeline_params(width: int, height: int, **kw) -> PipelineParams:
+    p = PipelineParams()
+    lib().craw_pipeline_params_init(C.byref(p))
+    p.width, p.height = width, height
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def frame_params(profile: Profile, **kw) -> FrameParams:
+    fp = FrameParams()
+    lib().craw_frame_params_init(C.byref(fp))
+    fp.profile = C.pointer(profile)
+    for k, v in kw.items():
+        if k == "noise_override":
+            v = NoiseModel(*v)
+        elif k == "illuminant":
+            v = Illuminant(*v)
+        setattr(fp, k, v)
+    return fp
+
+
+def image(data_ptr: int, pitch: int, fmt: int, width: int, height: int) -> Image:
+    return Image(data_ptr, pitch, fmt, width, height)
+
+
+def image_from_tensor(t, fmt: int) -> Image:
+    """A CRAWImage over a CUDA tensor: (h, w) uint16/int16 for R16_UNORM,
+    (h, w, 4) float32/float16 for RGBA32F/RGBA16F, rows contiguous."""
+    h, w = t.shape[0], t.shape[1]
+    return Image(t.data_ptr(), t.stride(0) * t.element_size(), fmt, w, h)
+
+
+# ---------------------------------------------------------------- objects
+
+class Context:
+    """A craw context on one CUDA device (craw_context_create)."""
+
+    def __init__(self, device: int = 0, log_level: int | None = None):
+        self._h = C.c_void_p()
+        params = CudaInitParams(device, None)
+        opts = ContextOptions()
+        opts.log_level = 2 if log_level is None else log_level
+        _check(lib().craw_context_create(C.byref(self._h), C.byref(params), C.byref(opts)),
+               "craw_context_create")
+        self.device = device
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self) -> None:
+        if self._h:
+            lib().craw_context_free(C.byref(self._h))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class AwbHistogram:
+    def __init__(self, count: np.ndarray, weight: np.ndarray, weight_bright: np.ndarray):
+        self.count, self.weight, self.weight_bright = count, weight, weight_bright
+
+
+class Pipeline:
+    """craw_pipeline_create / record / free over a :class:`Context`."""
+
+    def __init__(self, ctx: Context, params: PipelineParams):
+        self.ctx = ctx
+        self.params = params
+        self._h = C.c_void_p()
+        _check(lib().craw_pipeline_create(ctx.handle, C.byref(params), C.byref(self._h)),
+               "craw_pipeline_create")
+
+    def record(self, stream: int, src: Image, dst: Image, fp: FrameParams) -> None:
+        """Enqueues one frame on ``stream`` (a cudaStream_t as an int, e.g.
+        ``torch.cuda.current_stream().cuda_stream``)."""
+        _check(lib().craw_pipeline_record(self._h, C.c_void_p(stream), C.byref(src), C.byref(dst),
+                                          C.byref(fp)), "craw_pipeline_record")
+
+    def awb_histogram(self, frames_back: int = 0) -> AwbHistogram:
+        h = AwbHistogramC()
+        _check(lib().craw_pipeline_get_awb_histogram_n(self._h, frames_back, C.byref(h)),
+               "craw_pipeline_get_awb_histogram_n")
+        n = h.bins * h.bins
+
+        def arr(p):
+            return np.ctypeslib.as_array(p, shape=(n,)).reshape(h.bins, h.bins).copy()
+        return AwbHistogram(arr(h.count), arr(h.weight), arr(h.weight_bright))
+
+    def stage_times(self, frames_back: int = 0) -> list[tuple[str, int, float]]:
+        buf = (StageTime * 16)()
+        n = _check(lib().craw_pipeline_get_stage_times_n(self._h, frames_back, buf, 16),
+                   "craw_pipeline_get_stage_times_n")
+        return [(buf[i].name.decode(), buf[i].count, buf[i].ms) for i in range(n)]
+
+    def intermediate(self) -> tuple[Image, Image]:
+        rgb, mosaic = Image(), Image()
+        _check(lib().craw_pipeline_get_intermediate(self._h, C.byref(rgb), C.byref(mosaic)),
+               "craw_pipeline_get_intermediate")
+        return rgb, mosaic
+
+    def temporal_state(self) -> tuple[Image, Image]:
+        lvl, var = Image(), Image()
+        _check(lib().craw_pipeline_get_temporal_state(self._h, C.byref(lvl), C.byref(var)),
+               "craw_pipeline_get_temporal_state")
+        return lvl, var
+
+    def close(self) -> None:
+        if self._h:
+            lib().craw_pipeline_free(C.byref(self._h))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def debug_fail_alloc(k: int) -> None:
+    lib().craw_debug_fail_alloc(k)

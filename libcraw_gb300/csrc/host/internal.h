@@ -1,0 +1,45 @@
+/*
+ * Internals of the C23 host library: the context and pipeline objects and
+ * the host-side helpers the pipeline shares with the public functions.
+ */
+#ifndef CRAW_INTERNAL_H
+#define CRAW_INTERNAL_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#include <craw/pipeline.h>
+
+#include "../kabi.h"
+
+struct CRAWContext {
+    CRAWContextOptions opts;
+    int device;
+    int sm_count;
+    cudaMemPool_t pool;
+    bool own_pool;
+    cudaStream_t stream;     /* the context's own stream, for allocation only */
+};
+
+/* ACES 1.3 RGC constants (thresholds and solved scales). */
+typedef struct CRAWGamutCompress {
+    float thr[3];
+    float scl[3];
+    float pwr;
+    float inv_pwr;
+} CRAWGamutCompress;
+
+void craw_gamut_compress_params(CRAWGamutCompress *g);
+
+/* Device allocation from the context's pool on its own stream; counts
+ * allocations so a test can make the k-th one fail. */
+int craw_dev_alloc(CRAWContext *ctx, void **ptr, size_t bytes);
+void craw_dev_free(CRAWContext *ctx, void *ptr);
+int craw_dev_sync(CRAWContext *ctx);
+
+/* Bins one deferred AWB block on the host, with the CPU builder's
+ * arithmetic (lib/awb.c:270-291 of the reference). */
+void craw_awb_bin_host(float rr, float bb, float g, uint32_t *count, uint32_t *weight,
+                       uint32_t *weight_bright);
+
+#endif /* CRAW_INTERNAL_H */

@@ -1,0 +1,818 @@
+/*
+ * The pipeline: create, record, free, and the AWB and profiling readback
+ * (reference lib/pipeline.c:543-2415, re-designed for CUDA).
+ *
+ * A recording evaluates the frame's constants on the host, exactly as the
+ * reference does, and enqueues at most five kernels on the caller's
+ * stream:
+ *
+ *   denoise   mosaic (+ state) -> denoised mosaic (+ next state)
+ *   develop   mosaic -> dst directly (prep, debayer, colour and the AWB
+ *             block records fused); with the chroma denoise, mosaic ->
+ *             intermediate + quarter-resolution block means instead
+ *   [blur]    quarter -> filtered quarter
+ *   [up]      intermediate + quarters -> dst (+ AWB block records)
+ *   awb       block records -> histogram, then a copy into the pinned
+ *             host slot of this recording
+ *
+ * The library never synchronises the caller's stream. Intermediates come
+ * from a CUDA memory pool (cudaMallocFromPoolAsync on the context's own
+ * stream, which is synchronised once at the end of creation).
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <cuda_runtime_api.h>
+
+#include <craw/pipeline.h>
+
+#include "internal.h"
+
+static_assert(sizeof(CRAWPipelineParams) == 256, "CRAWPipelineParams size");
+static_assert(sizeof(CRAWFrameParams) == 264, "CRAWFrameParams size");
+static_assert(sizeof(CRAWContextOptions) == 1024, "CRAWContextOptions size");
+static_assert(sizeof(CRAWCudaInitParams) == 64, "CRAWCudaInitParams size");
+
+#define HIST_N (CRAW_AWB_HIST_BINS * CRAW_AWB_HIST_BINS)
+#define HIST_BYTES (3 * HIST_N * sizeof(uint32_t))
+#define DEFER_BYTES (CRAW_K_AWB_DEFER_MAX * sizeof(CRAWKAwbDeferred))
+
+/* Denoise constants, reference lib/pipeline.c:291-292. */
+#define DN_GUARD_LO 0.90f
+#define DN_GUARD_HI 1.00f
+
+#define MAX_STAGES 16
+
+enum { ST_DENOISE, ST_DEVELOP, ST_BLUR, ST_UP, ST_AWB, ST_NB };
+static const char *const stage_names[ST_NB] = {
+    "denoise_nlm", "develop", "chroma_blur", "chroma_up_color", "awb_reduce",
+};
+static const char *const plain_stage_names[ST_NB] = {
+    "plain_denoise", "plain_develop", "plain_chroma", "plain_chroma", "plain_awb",
+};
+
+/* One host-visible AWB slot: the three histograms, then the deferred
+ * blocks and their count, all pinned so one async copy fills them. */
+struct awb_slot {
+    uint8_t *host;            /* HIST_BYTES + DEFER_BYTES + 4 */
+    bool folded;              /* deferred blocks already binned */
+};
+
+struct prof_slot {
+    cudaEvent_t ev[MAX_STAGES][2];
+    int stage[MAX_STAGES];
+    uint32_t nb;
+};
+
+struct CRAWPipeline {
+    CRAWContext *ctx;
+    CRAWPipelineParams params;
+    bool has_denoise, has_temporal, has_chroma, awb, profile, keep, plain, fp16;
+    int dn_shape, dev_shape;
+
+    /* Device memory. */
+    uint16_t *clean;  size_t clean_pitch;
+    float *lvl[2];    size_t lvl_pitch;
+    uint8_t *var[2];  size_t var_pitch;
+    int tn_prev, tn_cur;
+    void *inter;      size_t inter_pitch;
+    void *q, *qf;     size_t q_pitch;
+    int qw, qh;
+    uint64_t *awb_rec;
+    uint8_t *awb_dev;         /* HIST_BYTES + DEFER_BYTES + 4, mirrors a slot */
+    uint32_t nb_blocks;
+
+    /* Plain-pipeline scratch. */
+    float *p_v, *p_scratch, *p_t, *p_var;
+
+    struct awb_slot slots[4];
+    uint32_t nb_slots;
+    uint64_t nb_recorded;
+    bool last_denoised;
+
+    struct prof_slot prof[CRAW_PIPELINE_PROFILE_SLOTS];
+    uint64_t prof_recorded;
+    CRAWStageTime prof_agg[MAX_STAGES];
+};
+
+static size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+CRAW_API void craw_pipeline_params_init(CRAWPipelineParams *p)
+{
+    if (!p)
+        return;
+    memset(p, 0, sizeof(*p));
+    p->cfa = CRAW_CFA_RGGB;
+    p->debayer = CRAW_DEBAYER_RCD;
+    p->out_space = CRAW_CS_XYZ_D65;
+    p->out_format = CRAW_FORMAT_RGBA16F;
+    p->nb_awb_slots = 1;
+}
+
+CRAW_API void craw_frame_params_init(CRAWFrameParams *fp)
+{
+    if (!fp)
+        return;
+    memset(fp, 0, sizeof(*fp));
+    fp->wb_mode = CRAW_WB_AS_SHOT;
+}
+
+static int alloc_pitched(CRAWPipeline *p, void **ptr, size_t *pitch, size_t row_bytes, uint32_t rows)
+{
+    size_t pt = align_up(row_bytes, 256);
+    if (pitch)
+        *pitch = pt;
+    return craw_dev_alloc(p->ctx, ptr, pt * rows);
+}
+
+static void release(CRAWPipeline *p)
+{
+    CRAWContext *ctx = p->ctx;
+    void *bufs[] = {
+        p->clean, p->lvl[0], p->lvl[1], p->var[0], p->var[1], p->inter, p->q, p->qf,
+        p->awb_rec, p->awb_dev, p->p_v, p->p_scratch, p->p_t, p->p_var,
+    };
+    cudaSetDevice(ctx->device);
+    for (size_t i = 0; i < CRAW_ARRAY_ELEMS(bufs); i++)
+        craw_dev_free(ctx, bufs[i]);
+    craw_dev_sync(ctx);
+    for (uint32_t i = 0; i < 4; i++)
+        if (p->slots[i].host)
+            cudaFreeHost(p->slots[i].host);
+    for (int s = 0; s < CRAW_PIPELINE_PROFILE_SLOTS; s++)
+        for (int i = 0; i < MAX_STAGES; i++)
+            for (int j = 0; j < 2; j++)
+                if (p->prof[s].ev[i][j])
+                    cudaEventDestroy(p->prof[s].ev[i][j]);
+    free(p);
+}
+
+CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *params,
+                                  CRAWPipeline **out)
+{
+    const uint32_t unsupported = CRAW_PIPELINE_FLAG_LENS | CRAW_PIPELINE_FLAG_FALSE_COLOR |
+                                 CRAW_PIPELINE_FLAG_HIGHLIGHT_RECONSTRUCTION |
+                                 CRAW_PIPELINE_FLAG_DEFRINGE | CRAW_PIPELINE_FLAG_SHARPEN;
+    CRAWPipeline *p;
+    uint32_t w, h;
+    int ret;
+
+    if (!ctx || !params || !out)
+        return CRAW_ERROR(EINVAL);
+    *out = NULL;
+    if (params->cfa != CRAW_CFA_RGGB) {
+        craw_log(ctx, CRAW_LOG_ERROR, "Only the RGGB CFA phase is implemented\n");
+        return CRAW_ERROR(ENOTSUP);
+    }
+    if (params->flags & unsupported) {
+        craw_log(ctx, CRAW_LOG_ERROR, "Pipeline flags 0x%x name stages this library does not "
+                 "build (lens, false colour, highlights, defringe, sharpening)\n",
+                 params->flags & unsupported);
+        return CRAW_ERROR(ENOTSUP);
+    }
+    w = params->width;
+    h = params->height;
+    if (!w || !h || (w & 1) || (h & 1) || w < 8 || h < 8) {
+        craw_log(ctx, CRAW_LOG_ERROR, "Invalid frame size %ux%u: both must be even and at least 8\n", w, h);
+        return CRAW_ERROR(EINVAL);
+    }
+    if (w > 32768 || h > 32768) {
+        craw_log(ctx, CRAW_LOG_ERROR, "Frame size %ux%u is larger than 32768 on a side\n", w, h);
+        return CRAW_ERROR(EINVAL);
+    }
+    if (params->out_format != CRAW_FORMAT_RGBA16F && params->out_format != CRAW_FORMAT_RGBA32F) {
+        craw_log(ctx, CRAW_LOG_ERROR, "Output format must be RGBA16F or RGBA32F\n");
+        return CRAW_ERROR(EINVAL);
+    }
+    if ((unsigned)params->debayer >= CRAW_DEBAYER_NB || (unsigned)params->out_space >= CRAW_CS_NB ||
+        (unsigned)params->storage > CRAW_STORAGE_FP16 || (unsigned)params->impl > CRAW_IMPL_PLAIN ||
+        params->nb_awb_slots > 4)
+        return CRAW_ERROR(EINVAL);
+
+    p = calloc(1, sizeof(*p));
+    if (!p)
+        return CRAW_ERROR(ENOMEM);
+    p->ctx = ctx;
+    p->params = *params;
+    p->awb = params->flags & CRAW_PIPELINE_FLAG_AWB_HISTOGRAM;
+    p->has_denoise = params->flags & CRAW_PIPELINE_FLAG_DENOISE;
+    p->has_temporal = params->flags & CRAW_PIPELINE_FLAG_TEMPORAL_DENOISE;
+    p->has_chroma = params->flags & CRAW_PIPELINE_FLAG_CHROMA_DENOISE;
+    p->profile = params->flags & CRAW_PIPELINE_FLAG_PROFILE;
+    p->keep = params->flags & CRAW_PIPELINE_FLAG_KEEP_INTERMEDIATE;
+    p->plain = params->impl == CRAW_IMPL_PLAIN;
+    p->fp16 = params->storage == CRAW_STORAGE_FP16 && !p->plain;
+    p->tn_prev = p->tn_cur = -1;
+    p->nb_slots = params->nb_awb_slots ? params->nb_awb_slots : 1;
+    p->qw = (int)((w + 3) / 4);
+    p->qh = (int)((h + 3) / 4);
+    p->dn_shape = CRAW_K_DN_SHAPE_2x8;
+
+    if ((p->has_denoise || p->has_temporal)) {
+        /* The plane mirror holds for one reflection of the search + patch
+         * radius (+1 for the temporal 3x3), reference pipeline.c:809-826. */
+        uint32_t dn_min = 2 * (3 + 1 + 1 + (p->has_temporal ? 1 : 0));
+        if (w < dn_min || h < dn_min) {
+            craw_log(ctx, CRAW_LOG_ERROR, "Denoising needs a frame of at least %ux%u, got %ux%u\n",
+                     dn_min, dn_min, w, h);
+            free(p);
+            return CRAW_ERROR(EINVAL);
+        }
+    }
+    if (p->has_chroma && (w < 20 || h < 20)) {
+        craw_log(ctx, CRAW_LOG_ERROR, "The chroma denoise needs a frame of at least 20x20\n");
+        free(p);
+        return CRAW_ERROR(EINVAL);
+    }
+
+    if ((ret = cudaSetDevice(ctx->device)) != cudaSuccess) {
+        free(p);
+        return CRAW_ERROR(EIO);
+    }
+
+    if (p->has_denoise || p->has_temporal)
+        if ((ret = alloc_pitched(p, (void **)&p->clean, &p->clean_pitch, (size_t)w * 2, h)) < 0)
+            goto fail;
+    if (p->has_temporal) {
+        for (int i = 0; i < 2; i++) {
+            if ((ret = alloc_pitched(p, (void **)&p->lvl[i], &p->lvl_pitch, (size_t)w * 4, h)) < 0 ||
+                (ret = alloc_pitched(p, (void **)&p->var[i], &p->var_pitch, (size_t)w, h)) < 0)
+                goto fail;
+        }
+    }
+    if (p->has_chroma || p->keep || p->plain) {
+        size_t bpp = p->fp16 ? 8 : 16;
+        if ((ret = alloc_pitched(p, &p->inter, &p->inter_pitch, (size_t)w * bpp, h)) < 0)
+            goto fail;
+    }
+    if (p->has_chroma) {
+        size_t bpp = p->fp16 ? 8 : 16;
+        if (p->plain)
+            bpp = 16;
+        if ((ret = alloc_pitched(p, &p->q, &p->q_pitch, (size_t)p->qw * bpp, (uint32_t)p->qh)) < 0 ||
+            (ret = alloc_pitched(p, &p->qf, NULL, (size_t)p->qw * bpp, (uint32_t)p->qh)) < 0)
+            goto fail;
+        if (p->plain)
+            p->q_pitch = (size_t)p->qw * 16;   /* the plain kernels index densely */
+    }
+    if (p->awb) {
+        p->nb_blocks = ((w + 7) / 8) * ((h + 7) / 8);
+        if ((ret = craw_dev_alloc(ctx, (void **)&p->awb_rec, (size_t)p->nb_blocks * 8)) < 0 ||
+            (ret = craw_dev_alloc(ctx, (void **)&p->awb_dev, HIST_BYTES + DEFER_BYTES + 16)) < 0)
+            goto fail;
+        for (uint32_t i = 0; i < p->nb_slots; i++) {
+            if (cudaHostAlloc((void **)&p->slots[i].host, HIST_BYTES + DEFER_BYTES + 16,
+                              cudaHostAllocDefault) != cudaSuccess) {
+                ret = CRAW_ERROR(ENOMEM);
+                goto fail;
+            }
+            memset(p->slots[i].host, 0, HIST_BYTES + DEFER_BYTES + 16);
+        }
+    }
+    if (p->plain) {
+        size_t n = (size_t)w * h;
+        if ((ret = craw_dev_alloc(ctx, (void **)&p->p_v, n * 4)) < 0)
+            goto fail;
+        if (params->debayer == CRAW_DEBAYER_RCD &&
+            (ret = craw_dev_alloc(ctx, (void **)&p->p_scratch, 7 * n * 4)) < 0)
+            goto fail;
+        if (p->has_denoise || p->has_temporal) {
+            if ((ret = craw_dev_alloc(ctx, (void **)&p->p_t, n * 4)) < 0 ||
+                (ret = craw_dev_alloc(ctx, (void **)&p->p_var, 3 * n * 4)) < 0)
+                goto fail;
+        }
+    }
+    if (p->profile) {
+        for (int s = 0; s < CRAW_PIPELINE_PROFILE_SLOTS; s++)
+            for (int i = 0; i < MAX_STAGES; i++)
+                for (int j = 0; j < 2; j++)
+                    if (cudaEventCreate(&p->prof[s].ev[i][j]) != cudaSuccess) {
+                        ret = CRAW_ERROR(ENOMEM);
+                        goto fail;
+                    }
+    }
+    if ((ret = craw_dev_sync(ctx)) < 0)
+        goto fail;
+    craw_log(ctx, CRAW_LOG_VERBOSE, "pipeline %ux%u debayer %d flags 0x%x storage %s impl %s\n",
+             w, h, params->debayer, params->flags, p->fp16 ? "fp16" : "fp32",
+             p->plain ? "plain" : "fused");
+    *out = p;
+    return 0;
+fail:
+    craw_log(ctx, CRAW_LOG_ERROR, "Pipeline allocation failed (%d)\n", ret);
+    release(p);
+    return ret < 0 ? ret : CRAW_ERROR(ENOMEM);
+}
+
+CRAW_API void craw_pipeline_free(CRAWPipeline **pp)
+{
+    if (!pp || !*pp)
+        return;
+    release(*pp);
+    *pp = NULL;
+}
+
+static int image_check(CRAWPipeline *p, const CRAWImage *img, CRAWFormat fmt, const char *what)
+{
+    size_t bpp = fmt == CRAW_FORMAT_R16_UNORM ? 2 : (fmt == CRAW_FORMAT_RGBA16F ? 8 : 16);
+    if (img->format != fmt) {
+        craw_log(p->ctx, CRAW_LOG_ERROR, "%s format %d, expected %d\n", what, (int)img->format, (int)fmt);
+        return CRAW_ERROR(EINVAL);
+    }
+    if (img->width != p->params.width || img->height != p->params.height) {
+        craw_log(p->ctx, CRAW_LOG_ERROR, "%s is %ux%u, pipeline %ux%u\n", what, img->width,
+                 img->height, p->params.width, p->params.height);
+        return CRAW_ERROR(EINVAL);
+    }
+    if (!img->data || ((uintptr_t)img->data & 15) || (img->pitch & 15) ||
+        img->pitch < (size_t)img->width * bpp) {
+        craw_log(p->ctx, CRAW_LOG_ERROR, "%s needs 16-byte aligned data and pitch >= width * %zu\n",
+                 what, bpp);
+        return CRAW_ERROR(EINVAL);
+    }
+    return 0;
+}
+
+/* The frame's noise model: override when a > 0, else the profile's table
+ * at as_shot_ei (reference lib/pipeline.c:1391-1409). */
+static int frame_noise_model(CRAWPipeline *p, const CRAWFrameParams *fp, CRAWNoiseModel *nm)
+{
+    int ret;
+    if (fp->noise_override.a > 0.0f) {
+        *nm = fp->noise_override;
+        return 0;
+    }
+    ret = craw_profile_noise_eval(fp->profile, fp->profile->as_shot_ei, nm);
+    if (ret < 0)
+        craw_log(p->ctx, CRAW_LOG_ERROR, "Denoising needs a noise model: the profile `%s` has no "
+                 "table and CRAWFrameParams.noise_override was not set\n",
+                 fp->profile->name[0] ? fp->profile->name : "(unnamed)");
+    return ret;
+}
+
+/* The denoise constants (reference lib/pipeline.c:1414-1467). */
+static int denoise_consts(CRAWPipeline *p, const CRAWFrameParams *fp, int mode, CRAWKDenoise *k)
+{
+    CRAWNoiseModel nm;
+    float a, b, c, h;
+    int ret = frame_noise_model(p, fp, &nm);
+    if (ret < 0)
+        return ret;
+    a = nm.a;
+    b = CRAW_MAX(nm.b, 0.0f);
+    if (!(a > 0.0f)) {
+        craw_log(p->ctx, CRAW_LOG_ERROR, "Noise model a = %g is not positive\n", (double)a);
+        return CRAW_ERROR(EINVAL);
+    }
+    c = 3.0f * a * a / 8.0f + b;
+    h = (mode & CRAW_K_DN_SPATIAL) ? fp->denoise_strength : 1.0f;
+    memset(k, 0, sizeof(*k));
+    k->pw = (int32_t)(p->params.width / 2);
+    k->ph = (int32_t)(p->params.height / 2);
+    k->gat_a = a;
+    k->gat_c = c;
+    k->gat_sc = sqrtf(c);
+    k->gat_fwd = 2.0f / a;
+    k->gat_inv = a / 4.0f;
+    k->gat_off = c / a;
+    k->gat_t0 = k->gat_fwd * k->gat_sc;
+    k->inv_h2 = 1.0f / (h * h);
+    k->t_alpha = (mode & CRAW_K_DN_TEMPORAL) ? fp->denoise_temporal_strength : 0.0f;
+    k->t_inv_h2 = 1.0f / (h * h);
+    k->guard_lo = DN_GUARD_LO;
+    k->guard_inv = 1.0f / (DN_GUARD_HI - DN_GUARD_LO);
+    k->mode = mode;
+    for (int s = 0; s < 4; s++) {
+        float range = fp->profile->white_level[s] - fp->profile->black_level[s];
+        k->black[s] = fp->profile->black_level[s];
+        k->inv_range[s] = 1.0f / range;
+        k->range[s] = range;
+    }
+    return 0;
+}
+
+static void mat3_mul_f(float out[3][3], const float a[3][3], const float b[3][3])
+{
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            out[i][j] = a[i][0] * b[0][j] + a[i][1] * b[1][j] + a[i][2] * b[2][j];
+}
+
+struct prof_ctx {
+    CRAWPipeline *p;
+    cudaStream_t s;
+    struct prof_slot *slot;
+};
+
+static void prof_begin(struct prof_ctx *pc, int stage)
+{
+    if (!pc->slot || pc->slot->nb >= MAX_STAGES)
+        return;
+    pc->slot->stage[pc->slot->nb] = stage;
+    cudaEventRecord(pc->slot->ev[pc->slot->nb][0], pc->s);
+}
+
+static void prof_end(struct prof_ctx *pc)
+{
+    if (!pc->slot || pc->slot->nb >= MAX_STAGES)
+        return;
+    cudaEventRecord(pc->slot->ev[pc->slot->nb][1], pc->s);
+    pc->slot->nb++;
+}
+
+CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWImage *src,
+                                  const CRAWImage *dst, const CRAWFrameParams *fp)
+{
+    CRAWContext *ctx;
+    CRAWColorParams frame;
+    CRAWKDevelop dk;
+    CRAWKDevelopIO dio;
+    CRAWKDenoise dnk;
+    CRAWKChroma ck;
+    CRAWGamutCompress gc;
+    struct prof_ctx pc = { 0 };
+    float m_out[3][3], scale;
+    bool spatial, temporal, replay, denoise, chroma;
+    int t_read, t_write, dn_mode = 0, ret;
+    enum CRAWColorSpace out_space;
+    const uint16_t *mosaic;
+    size_t mosaic_pitch;
+    uint32_t w, h;
+
+    if (!p || !src || !dst || !fp || !fp->profile)
+        return CRAW_ERROR(EINVAL);
+    ctx = p->ctx;
+    w = p->params.width;
+    h = p->params.height;
+    if ((ret = image_check(p, src, CRAW_FORMAT_R16_UNORM, "Source")) < 0 ||
+        (ret = image_check(p, dst, p->params.out_format, "Destination")) < 0)
+        return ret;
+    {
+        uintptr_t s0 = (uintptr_t)src->data, s1 = s0 + src->pitch * h;
+        uintptr_t d0 = (uintptr_t)dst->data, d1 = d0 + dst->pitch * h;
+        if (s0 < d1 && d0 < s1) {
+            craw_log(ctx, CRAW_LOG_ERROR, "Source and destination must not alias\n");
+            return CRAW_ERROR(EINVAL);
+        }
+    }
+
+    /* The prep applies the frame's own gains (reference pipeline.c:1773-1783). */
+    if ((ret = craw_profile_eval(fp->profile, fp->wb_mode, &fp->illuminant, &frame)) < 0)
+        return ret;
+    memset(&dk, 0, sizeof(dk));
+    dk.width = (int32_t)w;
+    dk.height = (int32_t)h;
+    dk.clip = 1.0f;
+    dk.method = p->params.debayer;
+    dk.fp16 = p->fp16;
+    for (int s4 = 0; s4 < 4; s4++) {
+        static const int chan[4] = { 0, 1, 1, 2 };
+        float range = fp->profile->white_level[s4] - fp->profile->black_level[s4];
+        if (!(range > 0.0f)) {
+            craw_log(ctx, CRAW_LOG_ERROR, "Profile site %d has white level %f <= black level %f\n",
+                     s4, fp->profile->white_level[s4], fp->profile->black_level[s4]);
+            return CRAW_ERROR(EINVAL);
+        }
+        dk.black[s4] = fp->profile->black_level[s4];
+        dk.range[s4] = range;
+        dk.wbs[s4] = frame.wb[chan[s4]];
+    }
+    for (int c = 0; c < 3; c++)
+        dk.awb_wb[c] = frame.wb[c];
+
+    /* Filters on or off for this frame, and the temporal sets (reference
+     * pipeline.c:1785-1818): a replay reads what the last recording read
+     * and rewrites what it wrote; a reset reads nothing. */
+    spatial = p->has_denoise && fp->denoise_strength > 0.0f;
+    temporal = p->has_temporal && fp->denoise_temporal_strength > 0.0f;
+    if (temporal && !(fp->denoise_temporal_strength <= 1.0f)) {
+        craw_log(ctx, CRAW_LOG_ERROR, "denoise_temporal_strength = %g; at most 1.0\n",
+                 (double)fp->denoise_temporal_strength);
+        return CRAW_ERROR(EINVAL);
+    }
+    replay = fp->denoise_temporal_replay;
+    t_read = replay ? p->tn_prev : p->tn_cur;
+    if (fp->flags & CRAW_FRAME_FLAG_TEMPORAL_RESET)
+        t_read = -1;
+    t_write = -1;
+    if (temporal)
+        t_write = replay && p->tn_cur >= 0 ? p->tn_cur : (t_read == 0 ? 1 : 0);
+    denoise = spatial || temporal;
+    if (denoise) {
+        dn_mode = (spatial ? CRAW_K_DN_SPATIAL : 0) | (temporal ? CRAW_K_DN_TEMPORAL : 0) |
+                  (temporal && t_read >= 0 ? CRAW_K_DN_HISTORY : 0);
+        if ((ret = denoise_consts(p, fp, dn_mode, &dnk)) < 0)
+            return ret;
+    }
+
+    chroma = p->has_chroma && fp->denoise_chroma_strength > 0.0f;
+    if (chroma && !(fp->denoise_chroma_strength <= 1.0f)) {
+        craw_log(ctx, CRAW_LOG_ERROR, "denoise_chroma_strength = %g; at most 1.0\n",
+                 (double)fp->denoise_chroma_strength);
+        return CRAW_ERROR(EINVAL);
+    }
+
+    /* Colour: M_out * cam_to_xyz * gain * 2^stops composed in float, RGC
+     * for ACEScg unless vetoed (reference pipeline.c:1899-1931). */
+    out_space = fp->out_space_set ? fp->out_space : p->params.out_space;
+    if ((ret = craw_colorspace_from_xyz_d65(out_space, m_out)) < 0) {
+        craw_log(ctx, CRAW_LOG_ERROR, "Unknown output colour space %d\n", (int)out_space);
+        return ret;
+    }
+    craw_gamut_compress_params(&gc);
+    mat3_mul_f(dk.color.m, m_out, frame.cam_to_xyz);
+    scale = frame.gain * exp2f(fp->exposure_stops);
+    for (int i = 0; i < 3; i++) {
+        for (int j = 0; j < 3; j++)
+            dk.color.m[i][j] *= scale;
+        dk.color.gc_thr[i] = gc.thr[i];
+        dk.color.gc_scl[i] = gc.scl[i];
+    }
+    dk.color.gc_pwr = gc.pwr;
+    dk.color.gc_inv_pwr = gc.inv_pwr;
+    dk.color.flags = (fp->flags & CRAW_FRAME_FLAG_CLAMP_NEGATIVE) ? CRAW_K_COLOR_CLAMP : 0;
+    if (out_space == CRAW_CS_ACES_AP1_LINEAR && !(fp->flags & CRAW_FRAME_FLAG_NO_GAMUT_COMPRESSION))
+        dk.color.flags |= CRAW_K_COLOR_RGC;
+
+    /* Nothing can fail on the host from here on. */
+    if (p->profile) {
+        pc.p = p;
+        pc.s = s;
+        pc.slot = &p->prof[p->prof_recorded % CRAW_PIPELINE_PROFILE_SLOTS];
+        pc.slot->nb = 0;
+    }
+
+    uint8_t *awb_hist = NULL;
+    CRAWKAwbOut awb = { 0 };
+    if (p->awb) {
+        awb_hist = p->awb_dev;
+        awb.rec = p->plain ? NULL : p->awb_rec;
+        awb.deferred = (CRAWKAwbDeferred *)(p->awb_dev + HIST_BYTES);
+        awb.nb_deferred = (uint32_t *)(p->awb_dev + HIST_BYTES + DEFER_BYTES);
+        if (cudaMemsetAsync(awb_hist, 0, HIST_BYTES, s) != cudaSuccess ||
+            cudaMemsetAsync(awb.nb_deferred, 0, 4, s) != cudaSuccess)
+            return CRAW_ERROR(EIO);
+    }
+
+    mosaic = src->data;
+    mosaic_pitch = src->pitch;
+    if (denoise) {
+        CRAWKDenoiseIO io = {
+            .src = src->data, .src_pitch = src->pitch,
+            .dst = p->clean, .dst_pitch = p->clean_pitch,
+            .lvl_pitch = p->lvl_pitch, .var_pitch = p->var_pitch,
+        };
+        if (temporal) {
+            if (t_read >= 0) {
+                io.lvl_prev = p->lvl[t_read];
+                io.var_prev = p->var[t_read];
+            }
+            io.lvl_next = p->lvl[t_write];
+            io.var_next = p->var[t_write];
+        }
+        prof_begin(&pc, ST_DENOISE);
+        ret = p->plain ? craw_k_plain_denoise(&dnk, &io, p->p_t, p->p_var, s)
+                       : craw_k_denoise(&dnk, &io, p->dn_shape, s);
+        prof_end(&pc);
+        if (ret < 0)
+            goto launch_fail;
+        mosaic = p->clean;
+        mosaic_pitch = p->clean_pitch;
+    }
+
+    memset(&dio, 0, sizeof(dio));
+    dio.src = mosaic;
+    dio.src_pitch = mosaic_pitch;
+    dio.awb = awb;
+    memset(&ck, 0, sizeof(ck));
+    ck.width = (int32_t)w;
+    ck.height = (int32_t)h;
+    ck.qw = p->qw;
+    ck.qh = p->qh;
+    ck.strength = fp->denoise_chroma_strength;
+    ck.fp16 = p->fp16;
+
+    if (p->plain) {
+        dio.dst = dst->data;
+        dio.dst_pitch = dst->pitch;
+        dio.dst_half = dst->format == CRAW_FORMAT_RGBA16F;
+        prof_begin(&pc, ST_DEVELOP);
+        ret = craw_k_plain_develop(&dk, &dio, chroma ? &ck : NULL, p->p_v, p->inter, p->inter_pitch,
+                                   p->p_scratch, p->q, p->qf, p->awb ? (uint32_t *)awb_hist : NULL, s);
+        prof_end(&pc);
+        if (ret < 0)
+            goto launch_fail;
+    } else if (!chroma) {
+        dio.dst = dst->data;
+        dio.dst_pitch = dst->pitch;
+        dio.dst_half = dst->format == CRAW_FORMAT_RGBA16F;
+        if (p->keep) {
+            dio.inter = p->inter;
+            dio.inter_pitch = p->inter_pitch;
+        }
+        prof_begin(&pc, ST_DEVELOP);
+        ret = craw_k_develop(&dk, &dio, p->dev_shape, s);
+        prof_end(&pc);
+        if (ret < 0)
+            goto launch_fail;
+    } else {
+        CRAWKAwbOut none = { 0 };
+        dio.inter = p->inter;
+        dio.inter_pitch = p->inter_pitch;
+        dio.quarter = p->q;
+        dio.quarter_pitch = p->q_pitch;
+        dio.awb = none;
+        prof_begin(&pc, ST_DEVELOP);
+        ret = craw_k_develop(&dk, &dio, p->dev_shape, s);
+        prof_end(&pc);
+        if (ret < 0)
+            goto launch_fail;
+        prof_begin(&pc, ST_BLUR);
+        ret = craw_k_chroma_blur(&ck, p->q, p->q_pitch, p->qf, p->q_pitch, s);
+        prof_end(&pc);
+        if (ret < 0)
+            goto launch_fail;
+        prof_begin(&pc, ST_UP);
+        ret = craw_k_chroma_up_color(&dk, &ck, p->inter, p->inter_pitch, p->q, p->qf, p->q_pitch,
+                                     dst->data, dst->pitch, dst->format == CRAW_FORMAT_RGBA16F,
+                                     p->keep ? p->inter : NULL, &awb, s);
+        prof_end(&pc);
+        if (ret < 0)
+            goto launch_fail;
+    }
+
+    if (p->awb) {
+        struct awb_slot *slot = &p->slots[p->nb_recorded % p->nb_slots];
+        if (!p->plain) {
+            prof_begin(&pc, ST_AWB);
+            ret = craw_k_awb_reduce(p->awb_rec, p->nb_blocks, (uint32_t *)awb_hist, s);
+            prof_end(&pc);
+            if (ret < 0)
+                goto launch_fail;
+        }
+        if (cudaMemcpyAsync(slot->host, p->awb_dev, HIST_BYTES + DEFER_BYTES + 4,
+                            cudaMemcpyDeviceToHost, s) != cudaSuccess) {
+            ret = CRAW_ERROR(EIO);
+            goto launch_fail;
+        }
+        slot->folded = false;
+        p->nb_recorded++;
+    }
+    if (p->profile)
+        p->prof_recorded++;
+    p->last_denoised = denoise;
+
+    /* Only now does the temporal state move (reference pipeline.c:2303-2313). */
+    if (p->has_temporal) {
+        p->tn_prev = t_read;
+        if (temporal)
+            p->tn_cur = t_write;
+        else if (!replay)
+            p->tn_cur = -1;
+    }
+    return 0;
+
+launch_fail:
+    /* A launch CUDA refused: the stream may hold part of this recording,
+     * so the temporal state is forgotten rather than trusted. */
+    craw_log(ctx, CRAW_LOG_ERROR, "Kernel launch failed: %s\n", cudaGetErrorString(cudaGetLastError()));
+    p->tn_prev = p->tn_cur = -1;
+    return CRAW_ERROR(EIO);
+}
+
+CRAW_API int craw_pipeline_get_awb_histogram_n(CRAWPipeline *p, uint32_t frames_back,
+                                               CRAWAwbHistogram *out)
+{
+    struct awb_slot *slot;
+    uint32_t *hist;
+
+    if (!p || !out)
+        return CRAW_ERROR(EINVAL);
+    if (!p->awb) {
+        craw_log(p->ctx, CRAW_LOG_ERROR, "Pipeline was created without CRAW_PIPELINE_FLAG_AWB_HISTOGRAM\n");
+        return CRAW_ERROR(EINVAL);
+    }
+    if (frames_back >= p->nb_slots || frames_back >= p->nb_recorded)
+        return CRAW_ERROR(EINVAL);
+    slot = &p->slots[(p->nb_recorded - 1 - frames_back) % p->nb_slots];
+    hist = (uint32_t *)slot->host;
+    if (!slot->folded) {
+        /* Bin the blocks the device deferred, with this host's logf. */
+        const CRAWKAwbDeferred *d = (const CRAWKAwbDeferred *)(slot->host + HIST_BYTES);
+        uint32_t nd = *(const uint32_t *)(slot->host + HIST_BYTES + DEFER_BYTES);
+        if (nd > CRAW_K_AWB_DEFER_MAX) {
+            craw_log(p->ctx, CRAW_LOG_WARN, "%u AWB blocks sat on bin edges; %u were binned on "
+                     "the device\n", nd, nd - CRAW_K_AWB_DEFER_MAX);
+            nd = CRAW_K_AWB_DEFER_MAX;
+        }
+        for (uint32_t i = 0; i < nd; i++)
+            craw_awb_bin_host(d[i].rr, d[i].bb, d[i].g, hist, hist + HIST_N, hist + 2 * HIST_N);
+        slot->folded = true;
+    }
+    out->bins = CRAW_AWB_HIST_BINS;
+    out->log_min = CRAW_AWB_HIST_LOG_MIN;
+    out->log_max = CRAW_AWB_HIST_LOG_MAX;
+    out->count = hist;
+    out->weight = hist + HIST_N;
+    out->weight_bright = hist + 2 * HIST_N;
+    return 0;
+}
+
+CRAW_API int craw_pipeline_get_awb_histogram(CRAWPipeline *p, CRAWAwbHistogram *out)
+{
+    return craw_pipeline_get_awb_histogram_n(p, 0, out);
+}
+
+CRAW_API int craw_pipeline_get_stage_times_n(CRAWPipeline *p, uint32_t frames_back,
+                                             CRAWStageTime *out, uint32_t max)
+{
+    struct prof_slot *slot;
+    uint32_t nb_agg = 0;
+
+    if (!p || (max && !out))
+        return CRAW_ERROR(EINVAL);
+    if (!p->profile) {
+        craw_log(p->ctx, CRAW_LOG_ERROR, "Pipeline was created without CRAW_PIPELINE_FLAG_PROFILE\n");
+        return CRAW_ERROR(EINVAL);
+    }
+    if (frames_back >= CRAW_PIPELINE_PROFILE_SLOTS || frames_back >= p->prof_recorded)
+        return CRAW_ERROR(EINVAL);
+    slot = &p->prof[(p->prof_recorded - 1 - frames_back) % CRAW_PIPELINE_PROFILE_SLOTS];
+    if (!slot->nb)
+        return 0;
+    /* Never blocks: a recording still in flight is EAGAIN. */
+    for (uint32_t i = 0; i < slot->nb; i++) {
+        cudaError_t e = cudaEventQuery(slot->ev[i][1]);
+        if (e == cudaErrorNotReady)
+            return CRAW_ERROR(EAGAIN);
+        if (e != cudaSuccess)
+            return CRAW_ERROR(EIO);
+    }
+    for (uint32_t i = 0; i < slot->nb; i++) {
+        const char *name = (p->plain ? plain_stage_names : stage_names)[slot->stage[i]];
+        float ms = 0.0f;
+        uint32_t j;
+        cudaEventElapsedTime(&ms, slot->ev[i][0], slot->ev[i][1]);
+        for (j = 0; j < nb_agg; j++)
+            if (!strcmp(p->prof_agg[j].name, name))
+                break;
+        if (j == nb_agg)
+            p->prof_agg[nb_agg++] = (CRAWStageTime) { .name = name };
+        p->prof_agg[j].count++;
+        p->prof_agg[j].ms += ms;
+    }
+    if (max)
+        memcpy(out, p->prof_agg, CRAW_MIN(max, nb_agg) * sizeof(*out));
+    return (int)nb_agg;
+}
+
+CRAW_API int craw_pipeline_get_stage_times(CRAWPipeline *p, CRAWStageTime *out, uint32_t max)
+{
+    return craw_pipeline_get_stage_times_n(p, 0, out, max);
+}
+
+CRAW_API int craw_pipeline_get_intermediate(CRAWPipeline *p, CRAWImage *rgb, CRAWImage *mosaic)
+{
+    if (!p || !p->keep)
+        return CRAW_ERROR(EINVAL);
+    if (rgb) {
+        rgb->data = p->inter;
+        rgb->pitch = p->inter_pitch;
+        rgb->format = p->fp16 ? CRAW_FORMAT_RGBA16F : CRAW_FORMAT_RGBA32F;
+        rgb->width = p->params.width;
+        rgb->height = p->params.height;
+    }
+    if (mosaic) {
+        mosaic->data = p->last_denoised ? p->clean : NULL;
+        mosaic->pitch = p->clean_pitch;
+        mosaic->format = CRAW_FORMAT_R16_UNORM;
+        mosaic->width = p->params.width;
+        mosaic->height = p->params.height;
+    }
+    return 0;
+}
+
+CRAW_API int craw_pipeline_get_temporal_state(CRAWPipeline *p, CRAWImage *level, CRAWImage *sqrt_var)
+{
+    if (!p || !p->has_temporal)
+        return CRAW_ERROR(EINVAL);
+    if (p->tn_cur < 0)
+        return CRAW_ERROR(EAGAIN);
+    if (level) {
+        level->data = p->lvl[p->tn_cur];
+        level->pitch = p->lvl_pitch;
+        level->format = (CRAWFormat)0;
+        level->width = p->params.width;
+        level->height = p->params.height;
+    }
+    if (sqrt_var) {
+        sqrt_var->data = p->var[p->tn_cur];
+        sqrt_var->pitch = p->var_pitch;
+        sqrt_var->format = (CRAWFormat)0;
+        sqrt_var->width = p->params.width;
+        sqrt_var->height = p->params.height;
+    }
+    return 0;
+}

@@ -1,0 +1,157 @@
+/*
+ * The thin C ABI between the C23 host library (csrc/host) and the sm_103a
+ * kernels (csrc/kernels). Plain structs of per-frame constants and plain
+ * device pointers; every launch is asynchronous on the given stream and
+ * returns 0 or a negative errno (CRAW_ERROR(EIO) when CUDA refuses the
+ * launch). Internal: not installed, not part of the public API.
+ */
+#ifndef CRAW_KABI_H
+#define CRAW_KABI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------ denoise */
+
+#define CRAW_K_DN_SPATIAL  1   /* non-local means */
+#define CRAW_K_DN_TEMPORAL 2   /* recursive average; writes the next state */
+#define CRAW_K_DN_HISTORY  4   /* the previous state is valid: read it */
+
+/* Per-frame constants of the temporal + VST + NLM pass (the reference's
+ * CRAWDenoisePush, lib/pipeline.c:1414-1467). */
+typedef struct CRAWKDenoise {
+    int32_t pw, ph;                  /* plane size: mosaic size / 2 */
+    float black[4], inv_range[4], range[4];   /* per quad site */
+    float gat_a, gat_c, gat_sc, gat_fwd, gat_inv, gat_off, gat_t0;
+    float inv_h2;                    /* 1 / strength^2 of the NLM */
+    float t_alpha, t_inv_h2;         /* temporal alpha_max and 1 / ht^2 */
+    float guard_lo, guard_inv;       /* highlight guard ramp */
+    int32_t mode;                    /* CRAW_K_DN_* */
+} CRAWKDenoise;
+
+typedef struct CRAWKDenoiseIO {
+    const uint16_t *src;  size_t src_pitch;   /* bytes */
+    uint16_t *dst;        size_t dst_pitch;
+    const float *lvl_prev; float *lvl_next;   size_t lvl_pitch;
+    const uint8_t *var_prev; uint8_t *var_next; size_t var_pitch;
+} CRAWKDenoiseIO;
+
+/* Tile shapes of the fused denoise kernel, chosen by the autotuner. */
+enum CRAWKDenoiseShape {
+    CRAW_K_DN_SHAPE_2x8 = 0,     /* a thread filters 2 columns x 8 rows */
+    CRAW_K_DN_SHAPE_2x4,         /* 2 columns x 4 rows */
+    CRAW_K_DN_SHAPE_NB,
+};
+
+int craw_k_denoise(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, int shape,
+                   cudaStream_t s);
+
+/* The plain baseline: one kernel for the transform and the temporal
+ * average into full FP32 planes (`t` and `var`, 4 planes of pw x ph each),
+ * and one straightforward NLM kernel reading them. */
+int craw_k_plain_denoise(const CRAWKDenoise *k, const CRAWKDenoiseIO *io,
+                         float *t, float *var, cudaStream_t s);
+
+/* ------------------------------------------------------------ develop */
+
+#define CRAW_K_COLOR_CLAMP 1u        /* clamp negatives */
+#define CRAW_K_COLOR_RGC   2u        /* ACES 1.3 gamut compression */
+
+/* The colour stage (the reference's CRAWColorPush, lib/pipeline.c:1905-1931). */
+typedef struct CRAWKColor {
+    float m[3][3];        /* rows of M_out * cam_to_xyz * gain * 2^stops */
+    float gc_thr[3], gc_scl[3], gc_pwr, gc_inv_pwr;
+    uint32_t flags;       /* CRAW_K_COLOR_* */
+} CRAWKColor;
+
+typedef struct CRAWKDevelop {
+    int32_t width, height;
+    float black[4], range[4], wbs[4];   /* per site; wbs = gain of the site's channel */
+    float clip;                         /* 1.0 */
+    int32_t method;                     /* CRAW_DEBAYER_* */
+    int32_t fp16;                       /* intermediate values rounded to half */
+    CRAWKColor color;
+    float awb_wb[3];                    /* white balance divided out of the block means */
+} CRAWKDevelop;
+
+/* One record per 8x8 block of the AWB histogram. 0 means "no sample".
+ * Otherwise bit 46 set, bits 0-13 the bin, 14-29 the 16.16 weight
+ * min(g, 0.5), 30-45 the 16.16 weight g^4. Blocks whose bin is within
+ * rounding of a bin edge are not binned on the device: their raw ratios go
+ * to the deferred list and the host bins them with its own logf, so the
+ * histogram is bit for bit the CPU builder's. */
+#define CRAW_K_AWB_VALID (1ull << 46)
+#define CRAW_K_AWB_DEFER_MAX 4096
+
+typedef struct CRAWKAwbDeferred {
+    float rr, bb, g;
+    uint32_t pad;
+} CRAWKAwbDeferred;
+
+typedef struct CRAWKAwbOut {
+    uint64_t *rec;                 /* ceil(w/8) * ceil(h/8) records, or NULL */
+    CRAWKAwbDeferred *deferred;    /* CRAW_K_AWB_DEFER_MAX entries */
+    uint32_t *nb_deferred;         /* counter, zeroed before the frame */
+} CRAWKAwbOut;
+
+typedef struct CRAWKDevelopIO {
+    const uint16_t *src; size_t src_pitch;
+    void *dst; size_t dst_pitch; int32_t dst_half;      /* NULL: no colour stage */
+    void *inter; size_t inter_pitch;                    /* NULL: not kept */
+    void *quarter; size_t quarter_pitch;                /* chroma: block means out */
+    CRAWKAwbOut awb;
+} CRAWKDevelopIO;
+
+/* Prep + debayer + (colour to dst | chroma block means) + AWB records +
+ * optional intermediate, in one kernel. */
+int craw_k_develop(const CRAWKDevelop *k, const CRAWKDevelopIO *io, int shape,
+                   cudaStream_t s);
+
+/* ------------------------------------------------------------- chroma */
+
+typedef struct CRAWKChroma {
+    int32_t width, height, qw, qh;
+    float strength;
+    int32_t fp16;
+} CRAWKChroma;
+
+/* 9x9 joint bilateral on the quarter grid: q -> qf. */
+int craw_k_chroma_blur(const CRAWKChroma *c, const void *q, size_t q_pitch,
+                       void *qf, size_t qf_pitch, cudaStream_t s);
+
+/* The band back into every pixel of the intermediate, then the AWB records
+ * and the colour stage; `inter_out` (optional) keeps the result. */
+int craw_k_chroma_up_color(const CRAWKDevelop *k, const CRAWKChroma *c,
+                           const void *inter, size_t inter_pitch,
+                           const void *q, const void *qf, size_t q_pitch,
+                           void *dst, size_t dst_pitch, int dst_half,
+                           void *inter_out, const CRAWKAwbOut *awb, cudaStream_t s);
+
+/* ---------------------------------------------------------------- awb */
+
+/* Folds `n` block records into the three 128^2 histograms (zeroed by the
+ * caller), through shared-memory histograms with warp-aggregated atomics. */
+int craw_k_awb_reduce(const uint64_t *rec, uint32_t n, uint32_t *hist, cudaStream_t s);
+
+/* ------------------------------------------------------- plain baseline */
+
+/* One straightforward FP32 kernel per stage, each through device memory:
+ * prep into `v` (w*h floats), debayer into `inter` (RGBA32F, pitch in
+ * bytes) using `scratch` (7 * w * h floats for RCD), chroma with `q`, `qf`
+ * (qw*qh*4 floats each), AWB by global atomics, colour into dst. */
+int craw_k_plain_develop(const CRAWKDevelop *k, const CRAWKDevelopIO *io,
+                         const CRAWKChroma *chroma, float *v, float *inter,
+                         size_t inter_pitch, float *scratch, float *q, float *qf,
+                         uint32_t *hist, cudaStream_t s);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* CRAW_KABI_H */

@@ -1,0 +1,73 @@
+/*
+ * The AWB histogram reduction: 8x8-block records (one u64 each, written by
+ * the develop kernels) folded into the three 128 x 128 histograms of the
+ * reference (count, sum of min(g, 0.5), sum of g^4; lib/awb.c:287-291).
+ *
+ * Each CTA keeps a private copy of all three histograms in shared memory
+ * (3 x 64 KB), folds a contiguous share of the records into it with
+ * warp-aggregated atomics (lanes holding the same bin are found with
+ * __match_any_sync and summed with __reduce_add_sync, so one leader does
+ * one shared atomic per distinct bin per warp), and finally adds its
+ * non-zero bins to the device histogram. Every sum is a uint32 sum, as in
+ * the reference, so the order of the additions does not matter.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr int kBins = 128 * 128;
+constexpr int kThreads = 1024;
+
+__global__ void __launch_bounds__(kThreads)
+k_awb_reduce(const uint64_t *__restrict__ rec, uint32_t n, uint32_t *__restrict__ hist)
+{
+    extern __shared__ uint32_t h[];
+    for (int i = threadIdx.x; i < 3 * kBins; i += kThreads)
+        h[i] = 0;
+    __syncthreads();
+
+    const uint32_t per = (n + gridDim.x - 1) / gridDim.x;
+    const uint32_t beg = blockIdx.x * per, end = min(n, beg + per);
+    const int lane = threadIdx.x & 31;
+    for (uint32_t base = beg; base < end; base += kThreads) {
+        uint32_t i = base + threadIdx.x;
+        uint64_t r = i < end ? __ldg(rec + i) : 0ull;
+        bool valid = (r & CRAW_K_AWB_VALID) != 0;
+        uint32_t bin = valid ? (uint32_t)(r & 0x3fffu) : 0xffffffffu;
+        uint32_t w = (uint32_t)((r >> 14) & 0xffffu), wb = (uint32_t)((r >> 30) & 0xffffu);
+        uint32_t group = __match_any_sync(0xffffffffu, bin);
+        uint32_t ws = __reduce_add_sync(group, w), bs = __reduce_add_sync(group, wb);
+        if (valid && lane == __ffs(group) - 1) {
+            atomicAdd(&h[bin], (uint32_t)__popc(group));
+            atomicAdd(&h[kBins + bin], ws);
+            atomicAdd(&h[2 * kBins + bin], bs);
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * kBins; i += kThreads) {
+        uint32_t v = h[i];
+        if (v)
+            atomicAdd(&hist[i], v);
+    }
+}
+
+} // namespace
+
+extern "C" int craw_k_awb_reduce(const uint64_t *rec, uint32_t n, uint32_t *hist, cudaStream_t s)
+{
+    static bool attr_set = false;
+    const int smem = 3 * kBins * (int)sizeof(uint32_t);
+    if (!attr_set) {
+        if (cudaFuncSetAttribute(k_awb_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
+            return -5;
+        attr_set = true;
+    }
+    /* About 4096 records a CTA, at most one CTA an SM of a 152-SM part. */
+    uint32_t grid = (n + 4095) / 4096;
+    grid = grid < 1 ? 1 : (grid > 148 ? 148 : grid);
+    k_awb_reduce<<<grid, kThreads, smem, s>>>(rec, n, hist);
+    return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}

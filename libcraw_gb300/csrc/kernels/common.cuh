@@ -1,0 +1,158 @@
+/*
+ * Device helpers shared by the sm_103a kernels: borders, the prep, the
+ * colour stage, the AWB block statistic and image stores.
+ */
+#pragma once
+
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "../kabi.h"
+
+#define CRAW_DEV __device__ __forceinline__
+
+/* Mirror without repeating the edge sample (reference common.glsl:49-55,
+ * lib/ref/ref_debayer.c:21-34), looping for tiles that hang further past
+ * a small frame than one reflection reaches. n >= 2. */
+CRAW_DEV int craw_mirror(int v, int n)
+{
+    while (v < 0 || v >= n) {
+        if (v < 0)
+            v = -v;
+        if (v >= n)
+            v = 2 * n - 2 - v;
+    }
+    return v;
+}
+
+/* The prep of one raw sample at quad site s (reference
+ * lib/ref/ref_debayer.c:42-63): UNORM, above black in units of the
+ * site's range, times the gain of its channel, clipped. Division, not a
+ * reciprocal, as the CPU reference divides. */
+CRAW_DEV float craw_prep(const CRAWKDevelop &k, uint16_t raw, int s)
+{
+    float r = (float)raw * (1.0f / 65535.0f);
+    float t = __fdiv_rn(__fsub_rn(r, k.black[s]), k.range[s]);
+    t = __fmul_rn(t, k.wbs[s]);
+    return t < k.clip ? t : k.clip;
+}
+
+/* 2^x on the MUFU. */
+CRAW_DEV float craw_ex2(float x)
+{
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+CRAW_DEV float craw_round_half(float x)
+{
+    return __half2float(__float2half_rn(x));
+}
+
+/* ACES 1.3 reference gamut compression of one AP1 triple (reference
+ * lib/gamut.c:61-92; a channel below its threshold is left untouched). */
+CRAW_DEV void craw_gamut_compress(const CRAWKColor &c, float o[3])
+{
+    float ach = fmaxf(o[0], fmaxf(o[1], o[2]));
+    if (ach == 0.0f)
+        return;
+    float mag = fabsf(ach);
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        float d = (ach - o[i]) / mag;
+        if (d < c.gc_thr[i])
+            continue;
+        float nd = (d - c.gc_thr[i]) / c.gc_scl[i];
+        float p = powf(nd, c.gc_pwr);
+        d = c.gc_thr[i] + c.gc_scl[i] * nd / powf(1.0f + p, c.gc_inv_pwr);
+        o[i] = ach - d * mag;
+    }
+}
+
+/* Matrix, gain and exposure to the output space, then the optional
+ * compression and clamp (reference lib/shaders/color.comp.glsl:72-91). */
+CRAW_DEV void craw_color(const CRAWKColor &c, const float in[3], float o[3])
+{
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+        o[r] = c.m[r][0] * in[0] + c.m[r][1] * in[1] + c.m[r][2] * in[2];
+    if (c.flags & CRAW_K_COLOR_RGC)
+        craw_gamut_compress(c, o);
+    if (c.flags & CRAW_K_COLOR_CLAMP) {
+#pragma unroll
+        for (int r = 0; r < 3; r++)
+            o[r] = fmaxf(o[r], 0.0f);
+    }
+}
+
+CRAW_DEV void craw_store_rgba(void *base, size_t pitch, int x, int y, int half_fmt,
+                              float r, float g, float b)
+{
+    char *row = (char *)base + (size_t)y * pitch;
+    if (half_fmt) {
+        __half2 lo = __floats2half2_rn(r, g), hi = __floats2half2_rn(b, 1.0f);
+        uint2 v;
+        v.x = *reinterpret_cast<uint32_t *>(&lo);
+        v.y = *reinterpret_cast<uint32_t *>(&hi);
+        reinterpret_cast<uint2 *>(row)[x] = v;
+    } else {
+        reinterpret_cast<float4 *>(row)[x] = make_float4(r, g, b, 1.0f);
+    }
+}
+
+CRAW_DEV void craw_load_rgb(const void *base, size_t pitch, int x, int y, int half_fmt,
+                            float o[3])
+{
+    const char *row = (const char *)base + (size_t)y * pitch;
+    if (half_fmt) {
+        uint2 v = reinterpret_cast<const uint2 *>(row)[x];
+        __half2 lo = *reinterpret_cast<__half2 *>(&v.x), hi = *reinterpret_cast<__half2 *>(&v.y);
+        float2 a = __half22float2(lo), b = __half22float2(hi);
+        o[0] = a.x; o[1] = a.y; o[2] = b.x;
+    } else {
+        float4 v = reinterpret_cast<const float4 *>(row)[x];
+        o[0] = v.x; o[1] = v.y; o[2] = v.z;
+    }
+}
+
+/* The AWB statistic of one block from its mean (reference
+ * lib/awb.c:255-291, whose operation order is kept so that the bins and
+ * weights are the CPU builder's bit for bit): skip clipped and near-black
+ * blocks, divide the gains back out, bin ln(R/G), ln(B/G) over
+ * [-2.5, 1] in 128 bins, weights min(g, 0.5) and g^4 in 16.16.
+ *
+ * The logarithm is taken in double and rounded once, which is the
+ * correctly rounded float log; a block whose bin position lies within
+ * 2e-4 of a bin edge, where a host logf an ulp away could choose the
+ * other bin, is deferred to the host instead. */
+CRAW_DEV uint64_t craw_awb_block(float r, float g, float b, const float wb[3],
+                                 CRAWKAwbDeferred *deferred, uint32_t *nb_deferred)
+{
+    const float lmin = -2.5f, lmax = 1.0f, span = lmax - lmin;
+    if (fmaxf(fmaxf(r, g), b) >= 0.98f || g < 0.002f)
+        return 0;
+    float rr = __fdiv_rn(__fdiv_rn(r, wb[0]), g);
+    float bb = __fdiv_rn(__fdiv_rn(b, wb[2]), g);
+    float x = (float)log((double)rr), y = (float)log((double)bb);
+    x = x > lmin ? (x < lmax ? x : lmax) : lmin;
+    y = y > lmin ? (y < lmax ? y : lmax) : lmin;
+    float fx = __fmul_rn(__fdiv_rn(__fsub_rn(x, lmin), span), 128.0f);
+    float fy = __fmul_rn(__fdiv_rn(__fsub_rn(y, lmin), span), 128.0f);
+    if (deferred && (fabsf(fx - rintf(fx)) < 2e-4f || fabsf(fy - rintf(fy)) < 2e-4f)) {
+        uint32_t i = atomicAdd(nb_deferred, 1u);
+        if (i < CRAW_K_AWB_DEFER_MAX) {
+            CRAWKAwbDeferred d;
+            d.rr = rr; d.bb = bb; d.g = g; d.pad = 0;
+            deferred[i] = d;
+            return 0;
+        }
+    }
+    int ix = (int)floorf(fx), iy = (int)floorf(fy);
+    ix = ix < 0 ? 0 : (ix > 127 ? 127 : ix);
+    iy = iy < 0 ? 0 : (iy > 127 ? 127 : iy);
+    float w = g < 0.5f ? g : 0.5f;
+    uint32_t wq = (uint32_t)roundf(__fmul_rn(w, 65536.0f));
+    uint32_t bq = (uint32_t)roundf(__fmul_rn(__fmul_rn(__fmul_rn(__fmul_rn(g, g), g), g), 65536.0f));
+    return CRAW_K_AWB_VALID | (uint64_t)(iy * 128 + ix) | ((uint64_t)wq << 14) | ((uint64_t)bq << 30);
+}

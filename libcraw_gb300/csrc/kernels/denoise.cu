@@ -1,0 +1,339 @@
+/*
+ * The raw-domain denoise: temporal recursive average + variance-
+ * stabilising transform + non-local means on the four CFA planes, in one
+ * launch (the reference's denoise_nlm pass; CPU definition
+ * lib/ref/ref_denoise.c:168-336).
+ *
+ * One CTA filters the same OX x OY tile of all four planes, i.e. a
+ * 2*OX x 2*OY region of the mosaic, so that the mosaic, the state and the
+ * outputs move as whole 2x2 quads with 32-bit (mosaic) and 64-bit (state)
+ * accesses. The stabilised planes of the tile and its search+patch apron
+ * live in shared memory as FP32.
+ *
+ * The search: a thread owns BW columns x M rows of one plane. For a
+ * search offset (dx, dy) it forms the squared differences of its own
+ * (BW+2) x (M+2) window against the shifted one, sums them along x and
+ * then along y in registers, and turns each of its BW*M patch distances
+ * into a weight with one ex2 on the MUFU. The shifted windows of one dx
+ * share all but one row between consecutive dy, so a column of the tile
+ * is read from shared memory once per dx for all seven dy.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+
+namespace {
+
+constexpr int S = 3;     /* search radius, reference lib/pipeline.c:261 */
+constexpr int P = 1;     /* patch radius, reference lib/pipeline.c:262 */
+constexpr float kLog2e = 1.4426950408889634f;
+constexpr float kVarMin = 1.0e-4f;
+
+CRAW_DEV float gat_fwd(const CRAWKDenoise &k, float u)
+{
+    if (u >= 0.0f)
+        return k.gat_fwd * sqrtf(k.gat_a * u + k.gat_c);
+    return k.gat_t0 + __fdiv_rn(u, k.gat_sc);
+}
+
+CRAW_DEV float gat_inv(const CRAWKDenoise &k, float t)
+{
+    if (t >= k.gat_t0)
+        return k.gat_inv * t * t - k.gat_off;
+    return (t - k.gat_t0) * k.gat_sc;
+}
+
+CRAW_DEV float level(const CRAWKDenoise &k, uint32_t raw, int pl)
+{
+    return ((float)raw * (1.0f / 65535.0f) - k.black[pl]) * k.inv_range[pl];
+}
+
+/* The four plane samples of mosaic quad (qx, qy): R, Gr, Gb, B. */
+CRAW_DEV void load_quad_u16(const CRAWKDenoiseIO &io, int qx, int qy, uint32_t q[4])
+{
+    const char *r0 = (const char *)io.src + (size_t)(2 * qy) * io.src_pitch;
+    uint32_t a = __ldg(reinterpret_cast<const uint32_t *>(r0) + qx);
+    uint32_t b = __ldg(reinterpret_cast<const uint32_t *>(r0 + io.src_pitch) + qx);
+    q[0] = a & 0xffffu; q[1] = a >> 16; q[2] = b & 0xffffu; q[3] = b >> 16;
+}
+
+CRAW_DEV void load_quad_f32(const float *base, size_t pitch, int qx, int qy, float q[4])
+{
+    const char *r0 = (const char *)base + (size_t)(2 * qy) * pitch;
+    float2 a = __ldg(reinterpret_cast<const float2 *>(r0) + qx);
+    float2 b = __ldg(reinterpret_cast<const float2 *>(r0 + pitch) + qx);
+    q[0] = a.x; q[1] = a.y; q[2] = b.x; q[3] = b.y;
+}
+
+template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY>
+struct Cfg {
+    static constexpr int R = SPATIAL ? S + P : 0;       /* apron of the tile */
+    static constexpr int OX = 16 * BW, OY = 2 * M * WP;  /* plane samples per tile */
+    static constexpr int TX = OX + 2 * R, TY = OY + 2 * R;
+    static constexpr int TS = (TX + 1) & ~1;             /* row stride, even for float2 */
+    static constexpr int TN = TY * TS;                   /* one plane's tile */
+    static constexpr int EX = TX + 2, EY = TY + 2;       /* history: one more ring */
+    static constexpr int EN = EX * EY;
+    static constexpr int NT = 4 * WP * 32;
+    static constexpr int smem_floats = 4 * TN * (HISTORY ? 2 : 1) + (HISTORY ? 8 * EN : 0);
+};
+
+template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY>
+__global__ void __launch_bounds__(Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>::NT)
+k_denoise(const CRAWKDenoise k, const CRAWKDenoiseIO io)
+{
+    using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>;
+    constexpr int R = C::R, OX = C::OX, OY = C::OY, TX = C::TX, TY = C::TY, TS = C::TS;
+    constexpr int NT = C::NT;
+    extern __shared__ __align__(16) float smem[];
+    float *T = smem;                                 /* 4 planes of TN */
+    float *V = smem + 4 * C::TN;                     /* history: variance left */
+    float *TC = smem + 8 * C::TN;                    /* history: this frame, apron R+1 */
+    float *TPv = TC + 4 * C::EN;                     /* history: last frame, apron R+1 */
+
+    const int tx0 = blockIdx.x * OX, ty0 = blockIdx.y * OY;
+    const int tid = threadIdx.x;
+
+    /* ---- fill: the stabilised tile, temporally averaged when there is a
+     * history (reference lib/ref/ref_denoise.c:244-296). */
+    if constexpr (!HISTORY) {
+        for (int i = tid; i < TX * TY; i += NT) {
+            int r = i / TX, c = i % TX;
+            int qy = craw_mirror(ty0 - R + r, k.ph), qx = craw_mirror(tx0 - R + c, k.pw);
+            uint32_t q[4];
+            load_quad_u16(io, qx, qy, q);
+#pragma unroll
+            for (int pl = 0; pl < 4; pl++)
+                T[pl * C::TN + r * TS + c] = gat_fwd(k, level(k, q[pl], pl));
+        }
+    } else {
+        for (int i = tid; i < C::EN; i += NT) {
+            int r = i / C::EX, c = i % C::EX;
+            int qy = craw_mirror(ty0 - R - 1 + r, k.ph), qx = craw_mirror(tx0 - R - 1 + c, k.pw);
+            uint32_t q[4];
+            float lp[4];
+            load_quad_u16(io, qx, qy, q);
+            load_quad_f32(io.lvl_prev, io.lvl_pitch, qx, qy, lp);
+#pragma unroll
+            for (int pl = 0; pl < 4; pl++) {
+                TC[pl * C::EN + i] = gat_fwd(k, level(k, q[pl], pl));
+                TPv[pl * C::EN + i] = gat_fwd(k, lp[pl]);
+            }
+        }
+        __syncthreads();
+        for (int i = tid; i < TX * TY; i += NT) {
+            int r = i / TX, c = i % TX;
+            int qy = craw_mirror(ty0 - R + r, k.ph), qx = craw_mirror(tx0 - R + c, k.pw);
+            const char *vr = (const char *)io.var_prev + (size_t)(2 * qy) * io.var_pitch;
+            uint16_t v0 = __ldg(reinterpret_cast<const uint16_t *>(vr) + qx);
+            uint16_t v1 = __ldg(reinterpret_cast<const uint16_t *>(vr + io.var_pitch) + qx);
+            uint32_t sv[4] = { v0 & 0xffu, (uint32_t)v0 >> 8, v1 & 0xffu, (uint32_t)v1 >> 8 };
+#pragma unroll
+            for (int pl = 0; pl < 4; pl++) {
+                const float *cp = TC + pl * C::EN, *pp = TPv + pl * C::EN;
+                int e0 = (r + 1) * C::EX + c + 1;
+                float d2 = 0.0f;
+#pragma unroll
+                for (int ky = -1; ky <= 1; ky++)
+#pragma unroll
+                    for (int kx = -1; kx <= 1; kx++) {
+                        float e = pp[e0 + ky * C::EX + kx] - cp[e0 + ky * C::EX + kx];
+                        d2 = __fadd_rn(d2, __fmul_rn(e, e));
+                    }
+                float x = d2 * (1.0f / 9.0f) * k.t_inv_h2 - 2.0f;
+                float a = k.t_alpha * expf(-fmaxf(x, 0.0f));
+                float sp = (float)sv[pl] * (1.0f / 255.0f);
+                float vv = __fadd_rn(__fmul_rn(1.0f - a, 1.0f - a), __fmul_rn(a * a, sp * sp));
+                T[pl * C::TN + r * TS + c] = __fadd_rn(__fmul_rn(cp[e0], 1.0f - a), __fmul_rn(pp[e0], a));
+                V[pl * C::TN + r * TS + c] = fmaxf(vv, kVarMin);
+            }
+        }
+    }
+    __syncthreads();
+
+    /* ---- the search */
+    const int warp = tid >> 5, lane = tid & 31;
+    const int pl = warp / WP, band = warp % WP;
+    const int ox0 = (lane & 15) * BW, oy0 = ((band << 1) | (lane >> 4)) * M;
+    const float *Tp = T + pl * C::TN;
+    float res[M][BW];
+
+    if constexpr (SPATIAL) {
+        const float *Vp = V + pl * C::TN;
+        float own[M + 2][BW + 2];
+        float acc[M][BW], wsum[M][BW], vc[M][BW], lvc[M][BW];
+#pragma unroll
+        for (int r = 0; r < M + 2; r++)
+#pragma unroll
+            for (int c = 0; c < BW + 2; c++)
+                own[r][c] = Tp[(oy0 + R - 1 + r) * TS + ox0 + R - 1 + c];
+        const float kd = (1.0f / 9.0f) * k.inv_h2;   /* inv_np * inv_h2 */
+        const float c1 = -kLog2e * kd, c0 = 2.0f * kLog2e;
+#pragma unroll
+        for (int m = 0; m < M; m++)
+#pragma unroll
+            for (int j = 0; j < BW; j++) {
+                acc[m][j] = 0.0f;
+                wsum[m][j] = 0.0f;
+                if constexpr (HISTORY) {
+                    vc[m][j] = Vp[(oy0 + R + m) * TS + ox0 + R + j];
+                    lvc[m][j] = __fdiv_rn(kLog2e, vc[m][j]);
+                }
+            }
+
+#pragma unroll
+        for (int dx = -S; dx <= S; dx++) {
+            /* The shifted column block for this dx, every row any dy reads. */
+            float win[M + 2 + 2 * S][BW + 2];
+            const int cs = ox0 + R - 1 + dx;
+#pragma unroll
+            for (int rr = 0; rr < M + 2 + 2 * S; rr++) {
+                const float *row = Tp + (oy0 + R - 1 - S + rr) * TS;
+                if (((R - 1 + dx) & 1) == 0) {
+#pragma unroll
+                    for (int c = 0; c < BW + 2; c += 2) {
+                        float2 t = *reinterpret_cast<const float2 *>(row + cs + c);
+                        win[rr][c] = t.x;
+                        win[rr][c + 1] = t.y;
+                    }
+                } else {
+                    float2 t = *reinterpret_cast<const float2 *>(row + cs - 1);
+                    win[rr][0] = t.y;
+#pragma unroll
+                    for (int c = 1; c < BW + 1; c += 2) {
+                        float2 u = *reinterpret_cast<const float2 *>(row + cs + c);
+                        win[rr][c] = u.x;
+                        win[rr][c + 1] = u.y;
+                    }
+                    win[rr][BW + 1] = *(row + cs + BW + 1);
+                }
+            }
+            float vq[HISTORY ? M + 2 * S : 1][BW];
+            if constexpr (HISTORY) {
+#pragma unroll
+                for (int rr = 0; rr < M + 2 * S; rr++) {
+                    const float *row = Vp + (oy0 + R - S + rr) * TS + ox0 + R + dx;
+#pragma unroll
+                    for (int j = 0; j < BW; j++)
+                        vq[rr][j] = row[j];
+                }
+            }
+#pragma unroll
+            for (int dy = -S; dy <= S; dy++) {
+                float hs[M + 2][BW];
+#pragma unroll
+                for (int r = 0; r < M + 2; r++) {
+                    float e[BW + 2];
+#pragma unroll
+                    for (int c = 0; c < BW + 2; c++) {
+                        float d = own[r][c] - win[r + dy + S][c];
+                        e[c] = d * d;
+                    }
+#pragma unroll
+                    for (int j = 0; j < BW; j++)
+                        hs[r][j] = e[j] + e[j + 1] + e[j + 2];
+                }
+#pragma unroll
+                for (int m = 0; m < M; m++) {
+#pragma unroll
+                    for (int j = 0; j < BW; j++) {
+                        float d2 = hs[m][j] + hs[m + 1][j] + hs[m + 2][j];
+                        float w;
+                        if constexpr (HISTORY)
+                            w = craw_ex2(fminf(fmaf(d2, -kd, vc[m][j] + vq[m + dy + S][j]) * lvc[m][j], 0.0f));
+                        else
+                            w = craw_ex2(fminf(fmaf(d2, c1, c0), 0.0f));
+                        wsum[m][j] += w;
+                        acc[m][j] = fmaf(w, win[m + 1 + dy + S][j + 1], acc[m][j]);
+                    }
+                }
+            }
+        }
+#pragma unroll
+        for (int m = 0; m < M; m++)
+#pragma unroll
+            for (int j = 0; j < BW; j++)
+                res[m][j] = __fdiv_rn(acc[m][j], wsum[m][j]);
+    }
+
+    /* ---- outputs: the next state, and the denoised mosaic in its raw
+     * encoding after the highlight guard (reference
+     * lib/ref/ref_denoise.c:285-324). */
+    const int px = pl & 1, py = pl >> 1;
+#pragma unroll
+    for (int m = 0; m < M; m++) {
+        const int qy = ty0 + oy0 + m;
+        if (qy >= k.ph)
+            break;
+#pragma unroll
+        for (int j = 0; j < BW; j++) {
+            const int qx = tx0 + ox0 + j;
+            if (qx >= k.pw)
+                continue;
+            const int my = 2 * qy + py, mx = 2 * qx + px;
+            const float tc = Tp[(oy0 + R + m) * TS + ox0 + R + j];
+            if constexpr (TEMPORAL) {
+                float *lr = (float *)((char *)io.lvl_next + (size_t)my * io.lvl_pitch);
+                uint8_t *vr = io.var_next + (size_t)my * io.var_pitch;
+                lr[mx] = gat_inv(k, tc);
+                if constexpr (HISTORY) {
+                    float vv = V[pl * C::TN + (oy0 + R + m) * TS + ox0 + R + j];
+                    vr[mx] = (uint8_t)rintf(sqrtf(fminf(fmaxf(vv, 0.0f), 1.0f)) * 255.0f);
+                } else {
+                    vr[mx] = 255;
+                }
+            }
+            float u = gat_inv(k, SPATIAL ? res[m][j] : tc);
+            uint16_t raw0 = __ldg((const uint16_t *)((const char *)io.src + (size_t)my * io.src_pitch) + mx);
+            float u0 = level(k, raw0, pl);
+            float gr = fminf(fmaxf((u0 - k.guard_lo) * k.guard_inv, 0.0f), 1.0f);
+            u = u + (u0 - u) * gr;
+            float ro = fminf(fmaxf(k.black[pl] + u * k.range[pl], 0.0f), 1.0f);
+            uint16_t *dr = (uint16_t *)((char *)io.dst + (size_t)my * io.dst_pitch);
+            dr[mx] = (uint16_t)rintf(ro * 65535.0f);
+        }
+    }
+}
+
+template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY>
+int launch(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, cudaStream_t s)
+{
+    using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>;
+    auto fn = k_denoise<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>;
+    const size_t smem = (size_t)C::smem_floats * sizeof(float);
+    static bool attr_set = false;   /* per process; the attribute is per function */
+    if (!attr_set) {
+        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+            return -5;
+        attr_set = true;
+    }
+    dim3 grid((k->pw + C::OX - 1) / C::OX, (k->ph + C::OY - 1) / C::OY);
+    fn<<<grid, C::NT, smem, s>>>(*k, *io);
+    return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}
+
+template <int BW, int M, int WP>
+int dispatch(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, cudaStream_t s)
+{
+    const bool sp = k->mode & CRAW_K_DN_SPATIAL, te = k->mode & CRAW_K_DN_TEMPORAL;
+    const bool hi = te && (k->mode & CRAW_K_DN_HISTORY);
+    if (sp && !te)  return launch<BW, M, WP, true, false, false>(k, io, s);
+    if (sp && !hi)  return launch<BW, M, WP, true, true, false>(k, io, s);
+    if (sp)         return launch<BW, M, WP, true, true, true>(k, io, s);
+    if (te && !hi)  return launch<BW, M, WP, false, true, false>(k, io, s);
+    if (te)         return launch<BW, M, WP, false, true, true>(k, io, s);
+    return -22;
+}
+
+} // namespace
+
+extern "C" int craw_k_denoise(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, int shape,
+                              cudaStream_t s)
+{
+    switch (shape) {
+    case CRAW_K_DN_SHAPE_2x8: return dispatch<2, 8, 1>(k, io, s);
+    case CRAW_K_DN_SHAPE_2x4: return dispatch<2, 4, 2>(k, io, s);
+    default:                  return -22;
+    }
+}

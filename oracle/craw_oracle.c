@@ -1,0 +1,442 @@
+/*
+ * CPU oracle for the frame-development path: a restatement of the
+ * reference's CPU implementation (lib/ref, and the host colour/noise/AWB
+ * code it calls), in float and in double.
+ *
+ * TEST INFRASTRUCTURE ONLY -- the checker, never the product. Only the
+ * tests, the smoke check and bench.py's CPU-baseline leg load it. The
+ * float instantiation is pinned against the reference's own build
+ * (oracle/_ref, tests/golden) by the CPU test suite.
+ *
+ * Compiled by __graft_entry__.build() with
+ *   gcc -std=c2x -O2 -fPIC -ffp-contract=off -fopenmp
+ * -ffp-contract=off keeps a*b+c unfused on every host (aarch64 gcc would
+ * otherwise contract to fma and drift from the x86 results).
+ */
+#include <errno.h>
+#include <math.h>
+#include <stdbool.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <craw/pipeline.h>
+
+#include "craw_oracle.h"
+
+#define ORC_API __attribute__((visibility("default")))
+
+/* ---------------------------------------------------- host constants */
+
+/* Profile evaluation, reference lib/profile.c:198-253 (knot intervals
+ * 160-196, computed in double and stored as float). */
+static void orc_knot_frac(double ca, double cb, double cct, double *frac)
+{
+    double f = 0.0;
+    if (cb > ca)
+        f = (cct - ca) / (cb - ca);
+    *frac = f < 0.0 ? 0.0 : (f > 1.0 ? 1.0 : f);
+}
+
+ORC_API int orc_profile_eval(const CRAWProfile *p, int mode, const CRAWIlluminant *illum,
+                             CRAWColorParams *out)
+{
+    if (!p || !out)
+        return -EINVAL;
+    if (mode == CRAW_WB_AS_SHOT) {
+        memcpy(out->wb, p->as_shot_wb, sizeof(out->wb));
+        memcpy(out->cam_to_xyz, p->as_shot_matrix, sizeof(out->cam_to_xyz));
+    } else if (mode == CRAW_WB_REBALANCE) {
+        double wb[3], cct, tg, f;
+        uint32_t i = 0, nb = p->nb_wb_knots;
+        if (!illum)
+            return -EINVAL;
+        if (!nb)
+            return -ENOTSUP;
+        if (!isfinite(illum->cct) || !isfinite(illum->tint))
+            return -EINVAL;
+        cct = (double)illum->cct;
+        cct = cct < p->wb_knots[0].cct ? p->wb_knots[0].cct :
+              (cct > p->wb_knots[nb - 1].cct ? p->wb_knots[nb - 1].cct : cct);
+        if (nb == 1) {
+            for (int c = 0; c < 3; c++)
+                wb[c] = p->wb_knots[0].wb[c];
+        } else {
+            while (i + 2 < nb && cct >= p->wb_knots[i + 1].cct)
+                i++;
+            orc_knot_frac(p->wb_knots[i].cct, p->wb_knots[i + 1].cct, cct, &f);
+            for (int c = 0; c < 3; c++) {
+                double a = p->wb_knots[i].wb[c], b = p->wb_knots[i + 1].wb[c];
+                wb[c] = a + (b - a) * f;
+            }
+        }
+        tg = exp((double)illum->tint * 0.70710678118654752440);
+        wb[0] *= tg;
+        wb[2] *= tg;
+        for (int c = 0; c < 3; c++)
+            out->wb[c] = (float)wb[c];
+        if (p->nb_matrix_knots) {
+            uint32_t nm = p->nb_matrix_knots, k = 0;
+            double mc = cct < p->matrix_knots[0].cct ? p->matrix_knots[0].cct :
+                        (cct > p->matrix_knots[nm - 1].cct ? p->matrix_knots[nm - 1].cct : cct);
+            if (nm == 1) {
+                memcpy(out->cam_to_xyz, p->matrix_knots[0].m, sizeof(float) * 9);
+            } else {
+                while (k + 2 < nm && mc >= p->matrix_knots[k + 1].cct)
+                    k++;
+                orc_knot_frac(p->matrix_knots[k].cct, p->matrix_knots[k + 1].cct, mc, &f);
+                for (int r = 0; r < 3; r++)
+                    for (int c = 0; c < 3; c++) {
+                        double a = p->matrix_knots[k].m[r][c], b = p->matrix_knots[k + 1].m[r][c];
+                        out->cam_to_xyz[r][c] = (float)(a + (b - a) * f);
+                    }
+            }
+        } else {
+            memcpy(out->cam_to_xyz, p->as_shot_matrix, sizeof(out->cam_to_xyz));
+        }
+    } else {
+        return -EINVAL;
+    }
+    out->gain = p->gain;
+    if (p->as_shot_ei > 0.0f && p->exposure_index > 0.0f)
+        out->gain *= p->exposure_index / p->as_shot_ei;
+    return 0;
+}
+
+/* Colour-space matrices in double, reference lib/colorspace.c:20-270:
+ * published primaries, D65 (0.3127, 0.3290), the ACES white
+ * (0.32168, 0.33767) and the Bradford cone matrix. */
+static const double orc_prim[CRAW_CS_NB][3][2] = {
+    [CRAW_CS_BT709_LINEAR]    = { { 0.64, 0.33 }, { 0.30, 0.60 }, { 0.15, 0.06 } },
+    [CRAW_CS_BT2020_LINEAR]   = { { 0.708, 0.292 }, { 0.170, 0.797 }, { 0.131, 0.046 } },
+    [CRAW_CS_P3D65_LINEAR]    = { { 0.680, 0.320 }, { 0.265, 0.690 }, { 0.150, 0.060 } },
+    [CRAW_CS_V_GAMUT_LINEAR]  = { { 0.730, 0.280 }, { 0.165, 0.840 }, { 0.100, -0.030 } },
+    [CRAW_CS_ACES_AP0_LINEAR] = { { 0.7347, 0.2653 }, { 0.0, 1.0 }, { 0.0001, -0.0770 } },
+    [CRAW_CS_ACES_AP1_LINEAR] = { { 0.713, 0.293 }, { 0.165, 0.830 }, { 0.128, 0.044 } },
+};
+
+static void orc_xyz(double x, double y, double o[3])
+{
+    o[0] = x / y;
+    o[1] = 1.0;
+    o[2] = (1.0 - x - y) / y;
+}
+
+static void orc_mul(const double a[3][3], const double b[3][3], double o[3][3])
+{
+    double t[3][3];
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            t[i][j] = a[i][0] * b[0][j] + a[i][1] * b[1][j] + a[i][2] * b[2][j];
+    memcpy(o, t, sizeof(t));
+}
+
+static void orc_mulv(const double m[3][3], const double v[3], double o[3])
+{
+    double t[3];
+    for (int i = 0; i < 3; i++)
+        t[i] = m[i][0] * v[0] + m[i][1] * v[1] + m[i][2] * v[2];
+    memcpy(o, t, sizeof(t));
+}
+
+static int orc_inv(const double m[3][3], double o[3][3])
+{
+    double det = m[0][0] * (m[1][1] * m[2][2] - m[1][2] * m[2][1])
+               - m[0][1] * (m[1][0] * m[2][2] - m[1][2] * m[2][0])
+               + m[0][2] * (m[1][0] * m[2][1] - m[1][1] * m[2][0]);
+    double t[3][3];
+    if (!(fabs(det) > 1e-12))
+        return -EINVAL;
+    t[0][0] = (m[1][1] * m[2][2] - m[1][2] * m[2][1]) / det;
+    t[0][1] = (m[0][2] * m[2][1] - m[0][1] * m[2][2]) / det;
+    t[0][2] = (m[0][1] * m[1][2] - m[0][2] * m[1][1]) / det;
+    t[1][0] = (m[1][2] * m[2][0] - m[1][0] * m[2][2]) / det;
+    t[1][1] = (m[0][0] * m[2][2] - m[0][2] * m[2][0]) / det;
+    t[1][2] = (m[0][2] * m[1][0] - m[0][0] * m[1][2]) / det;
+    t[2][0] = (m[1][0] * m[2][1] - m[1][1] * m[2][0]) / det;
+    t[2][1] = (m[0][1] * m[2][0] - m[0][0] * m[2][1]) / det;
+    t[2][2] = (m[0][0] * m[1][1] - m[0][1] * m[1][0]) / det;
+    memcpy(o, t, sizeof(t));
+    return 0;
+}
+
+static int orc_rgb_to_xyz(const double prim[3][2], const double white[2], double o[3][3])
+{
+    double p[3][3], inv[3][3], w[3], s[3];
+    for (int c = 0; c < 3; c++) {
+        double col[3];
+        orc_xyz(prim[c][0], prim[c][1], col);
+        for (int i = 0; i < 3; i++)
+            p[i][c] = col[i];
+    }
+    orc_xyz(white[0], white[1], w);
+    if (orc_inv(p, inv) < 0)
+        return -EINVAL;
+    orc_mulv(inv, w, s);
+    for (int i = 0; i < 3; i++)
+        for (int c = 0; c < 3; c++)
+            o[i][c] = p[i][c] * s[c];
+    return 0;
+}
+
+static int orc_bradford(const double src[2], const double dst[2], double o[3][3])
+{
+    static const double bfd[3][3] = {
+        {  0.8951,  0.2664, -0.1614 },
+        { -0.7502,  1.7135,  0.0367 },
+        {  0.0389, -0.0685,  1.0296 },
+    };
+    double bi[3][3], sc[3][3] = { { 0 } }, t[3][3], ws[3], wd[3], cs[3], cd[3];
+    orc_xyz(src[0], src[1], ws);
+    orc_xyz(dst[0], dst[1], wd);
+    orc_mulv(bfd, ws, cs);
+    orc_mulv(bfd, wd, cd);
+    for (int i = 0; i < 3; i++) {
+        if (!(fabs(cs[i]) > 1e-12))
+            return -EINVAL;
+        sc[i][i] = cd[i] / cs[i];
+    }
+    if (orc_inv(bfd, bi) < 0)
+        return -EINVAL;
+    orc_mul(sc, bfd, t);
+    orc_mul(bi, t, o);
+    return 0;
+}
+
+static int orc_colorspace_to_xyz_d(int cs, double o[3][3])
+{
+    static const double d65[2] = { 0.3127, 0.3290 }, aces[2] = { 0.32168, 0.33767 };
+    bool aw;
+    double m[3][3];
+
+    if (cs < 0 || cs >= CRAW_CS_NB)
+        return -EINVAL;
+    if (cs == CRAW_CS_XYZ_D65) {
+        for (int i = 0; i < 3; i++)
+            for (int j = 0; j < 3; j++)
+                o[i][j] = i == j;
+        return 0;
+    }
+    aw = cs == CRAW_CS_ACES_AP0_LINEAR || cs == CRAW_CS_ACES_AP1_LINEAR;
+    if (orc_rgb_to_xyz(orc_prim[cs], aw ? aces : d65, m) < 0)
+        return -EINVAL;
+    if (aw) {
+        double cat[3][3];
+        if (orc_bradford(aces, d65, cat) < 0)
+            return -EINVAL;
+        orc_mul(cat, m, m);
+    }
+    memcpy(o, m, sizeof(m));
+    return 0;
+}
+
+ORC_API int orc_colorspace_from_xyz_d(int cs, double o[3][3])
+{
+    double to[3][3];
+    int ret = orc_colorspace_to_xyz_d(cs, to);
+    if (ret < 0)
+        return ret;
+    return orc_inv(to, o);
+}
+
+ORC_API int orc_colorspace_from_xyz_f(int cs, float o[3][3])
+{
+    double m[3][3];
+    int ret = orc_colorspace_from_xyz_d(cs, m);
+    if (ret < 0)
+        return ret;
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++)
+            o[i][j] = (float)m[i][j];
+    return 0;
+}
+
+/* ACES 1.3 RGC constants from the Academy's CTL, scales solved in double,
+ * reference lib/gamut.c:21-59. */
+ORC_API void orc_gamut_params(struct orc_gamut *g)
+{
+    static const double lim[3] = { 1.147, 1.264, 1.312 };
+    static const double thr[3] = { 0.815, 0.803, 0.880 };
+    const double pwr = 1.2;
+    for (int i = 0; i < 3; i++) {
+        g->thr[i] = (float)thr[i];
+        g->scl[i] = (float)((lim[i] - thr[i]) /
+                            pow(pow((1.0 - thr[i]) / (lim[i] - thr[i]), -pwr) - 1.0, 1.0 / pwr));
+    }
+    g->pwr = (float)pwr;
+    g->inv_pwr = (float)(1.0 / pwr);
+}
+
+/* Noise table evaluation, reference lib/noise.c:37-110. */
+ORC_API int orc_noise_model_eval(const CRAWNoiseKnot *k, uint32_t n, float iso, CRAWNoiseModel *out)
+{
+    uint32_t i;
+    float t;
+    if (!k || !n || !out)
+        return -EINVAL;
+    if (!(iso > 0.0f) || !isfinite(iso)) {
+        out->a = k[0].a;
+        out->b = k[0].b;
+        return 0;
+    }
+    if (iso <= k[0].iso) {
+        out->a = k[0].a * (iso / k[0].iso);
+        out->b = k[0].b;
+        return 0;
+    }
+    if (iso >= k[n - 1].iso) {
+        float g = iso / k[n - 1].iso;
+        out->a = k[n - 1].a * g;
+        out->b = k[n - 1].b * g * g;
+        return 0;
+    }
+    for (i = 0; i + 1 < n; i++)
+        if (iso <= k[i + 1].iso)
+            break;
+    if (!(k[i + 1].iso > k[i].iso)) {
+        out->a = k[i].a;
+        out->b = k[i].b;
+        return 0;
+    }
+    t = (logf(iso) - logf(k[i].iso)) / (logf(k[i + 1].iso) - logf(k[i].iso));
+    if (k[i].a > 0.0f && k[i + 1].a > 0.0f)
+        out->a = expf(logf(k[i].a) + t * (logf(k[i + 1].a) - logf(k[i].a)));
+    else
+        out->a = k[i].a + t * (k[i + 1].a - k[i].a);
+    if (k[i].b > 0.0f && k[i + 1].b > 0.0f)
+        out->b = expf(logf(k[i].b) + t * (logf(k[i + 1].b) - logf(k[i].b)));
+    else
+        out->b = k[i].b + t * (k[i + 1].b - k[i].b);
+    return 0;
+}
+
+/* The frame's noise model: the override when a > 0, else the profile's
+ * table at as_shot_ei; reference lib/ref/ref_color.c:78-89,
+ * lib/noise.c:112-123. */
+ORC_API int orc_noise_model(const CRAWFrameParams *fp, CRAWNoiseModel *out)
+{
+    const CRAWProfile *p;
+    float iso;
+    if (!fp || !fp->profile || !out)
+        return -EINVAL;
+    if (fp->noise_override.a > 0.0f) {
+        *out = fp->noise_override;
+        return 0;
+    }
+    p = fp->profile;
+    if (!p->nb_noise_knots)
+        return -ENOTSUP;
+    iso = p->as_shot_ei;
+    return orc_noise_model_eval(p->noise_knots, p->nb_noise_knots, iso, out);
+}
+
+/* AWB histogram of 8x8 block means, reference lib/awb.c:213-296. */
+ORC_API int orc_awb_histogram(const float *rgb, uint32_t width, uint32_t height, size_t stride,
+                              int channels, const float wb[3], uint32_t *count,
+                              uint32_t *weight, uint32_t *weight_bright)
+{
+    const uint32_t bins = 128;
+    const float lmin = -2.5f, lmax = 1.0f;
+
+    if (!rgb || !wb || !count || !weight || !weight_bright)
+        return -EINVAL;
+    if (channels != 3 && channels != 4)
+        return -EINVAL;
+    if (stride < (size_t)width * (size_t)channels)
+        return -EINVAL;
+    if (!(wb[0] > 0.0f) || !(wb[2] > 0.0f))
+        return -EINVAL;
+    memset(count, 0, (size_t)bins * bins * 4);
+    memset(weight, 0, (size_t)bins * bins * 4);
+    memset(weight_bright, 0, (size_t)bins * bins * 4);
+    for (uint32_t by = 0; by < height; by += 8) {
+        uint32_t y1 = by + 8 < height ? by + 8 : height;
+        for (uint32_t bx = 0; bx < width; bx += 8) {
+            uint32_t x1 = bx + 8 < width ? bx + 8 : width;
+            float acc[3] = { 0.0f, 0.0f, 0.0f };
+            float n = (float)((y1 - by) * (x1 - bx));
+            float r, g, b, rr, bb, x, y, w, span = lmax - lmin;
+            int ix, iy;
+            for (uint32_t py = by; py < y1; py++) {
+                const float *row = rgb + (size_t)py * stride;
+                for (uint32_t px = bx; px < x1; px++) {
+                    acc[0] += row[(size_t)px * channels + 0];
+                    acc[1] += row[(size_t)px * channels + 1];
+                    acc[2] += row[(size_t)px * channels + 2];
+                }
+            }
+            r = acc[0] / n;
+            g = acc[1] / n;
+            b = acc[2] / n;
+            if (fmaxf(fmaxf(r, g), b) >= 0.98f || g < 0.002f)
+                continue;
+            rr = (r / wb[0]) / g;
+            bb = (b / wb[2]) / g;
+            x = logf(rr);
+            y = logf(bb);
+            x = x > lmin ? (x < lmax ? x : lmax) : lmin;
+            y = y > lmin ? (y < lmax ? y : lmax) : lmin;
+            ix = (int)floorf((x - lmin) / span * bins);
+            iy = (int)floorf((y - lmin) / span * bins);
+            ix = ix < 0 ? 0 : (ix > (int)bins - 1 ? (int)bins - 1 : ix);
+            iy = iy < 0 ? 0 : (iy > (int)bins - 1 ? (int)bins - 1 : iy);
+            w = g < 0.5f ? g : 0.5f;
+            count[iy * bins + ix] += 1;
+            weight[iy * bins + ix] += (uint32_t)roundf(w * 65536.0f);
+            weight_bright[iy * bins + ix] += (uint32_t)roundf(g * g * g * g * 65536.0f);
+        }
+    }
+    return 0;
+}
+
+/* ------------------------------------------------- the two instantiations */
+
+static inline float orc_mstore_f32(double x) { return (float)x; }
+static inline double orc_mstore_f64(double x) { return x; }
+
+#define R float
+#define SFX(n) ORC_API_F32(n)
+#define ORC_API_F32(n) n##_f32
+#define R_SQRT sqrtf
+#define R_EXP expf
+#define R_EXP2 exp2f
+#define R_LOG logf
+#define R_POW powf
+#define R_RINT rintf
+#define R_FABS fabsf
+#define R_FLOOR floorf
+#include "oracle_impl.h"
+#undef R
+#undef SFX
+#undef R_SQRT
+#undef R_EXP
+#undef R_EXP2
+#undef R_LOG
+#undef R_POW
+#undef R_RINT
+#undef R_FABS
+#undef R_FLOOR
+#undef ORC_DN_S
+#undef ORC_DN_P
+#undef ORC_DN_GUARD_LO
+#undef ORC_DN_GUARD_HI
+#undef ORC_DN_VAR_MIN
+#undef ORC_RCD_EPS
+#undef ORC_CD_RADIUS
+#undef ORC_CD_INV_2S2
+#undef ORC_CD_RANGE_K
+#undef ORC_CD_CHROMA_K
+#undef ORC_CD_RANGE_EPS
+
+#define R double
+#define SFX(n) ORC_API_F64(n)
+#define ORC_API_F64(n) n##_f64
+#define R_SQRT sqrt
+#define R_EXP exp
+#define R_EXP2 exp2
+#define R_LOG log
+#define R_POW pow
+#define R_RINT rint
+#define R_FABS fabs
+#define R_FLOOR floor
+#include "oracle_impl.h"

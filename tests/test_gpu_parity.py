@@ -1,0 +1,258 @@
+"""GPU parity: every stage of the path through the C ABI (libcraw.so) against
+the CPU oracle on the same seeded inputs, at sizes the oracle finishes in
+seconds.
+
+Tolerances (the metric of reference tests/test_pipeline.c:321-359,
+per-pixel magnitude-relative error floored at 1% of the frame peak):
+  * FP32 storage vs the float oracle: 2e-4 (bilinear, MHC), 1e-3 (RCD),
+    the differences being fused multiply-adds and division order;
+  * FP16 storage vs the float oracle: 2e-3 (one half-float rounding of the
+    intermediate, 4.9e-4 relative, carried through the 3x3 matrix);
+  * with the denoise: the denoised mosaic within one 16-bit code of the
+    oracle's, and the output within 2e-3;
+  * against the double oracle: 1e-3 for FP32 storage (the target).
+AWB histograms are compared for exact equality with the CPU builder run on
+the intermediate the GPU produced.
+"""
+import numpy as np
+import pytest
+import torch
+
+import libcraw_gb300 as L
+from libcraw_gb300 import workloads as W
+from oracle import Oracle, max_abs, max_rel, psnr
+
+pytestmark = pytest.mark.gpu
+
+orc = Oracle()
+TOL_FP32 = {L.DEBAYER_BILINEAR: 2e-4, L.DEBAYER_MHC: 2e-4, L.DEBAYER_RCD: 1e-3}
+TOL_FP16 = 2e-3
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = L.Context(0)
+    yield c
+    c.close()
+
+
+def run(ctx, m, pp, fp, fmt=L.FORMAT_RGBA32F):
+    from gpu_util import develop
+    with L.Pipeline(ctx, pp) as pipe:
+        return develop(pipe, m, fp, fmt)
+
+
+def frame(w, h, seed, a=4.0, b=40.0, **kw):
+    return W.synth_frame(w, h, seed, rects=10, zone_plates=1, noise_a_dn=a, noise_b_dn=b, **kw)
+
+
+@pytest.mark.parametrize("storage", [L.STORAGE_FP32, L.STORAGE_FP16])
+@pytest.mark.parametrize("deb", [L.DEBAYER_BILINEAR, L.DEBAYER_MHC, L.DEBAYER_RCD])
+@pytest.mark.parametrize("cs", [L.CS_BT709, L.CS_ACES_AP1])
+def test_develop_vs_oracle(ctx, deb, cs, storage):
+    w, h = 200, 136
+    m = frame(w, h, 10 + deb)
+    prof = W.make_profile()
+    pp = L.pipeline_params(w, h, debayer=deb, out_space=cs, out_format=L.FORMAT_RGBA32F,
+                           storage=storage)
+    fp = L.frame_params(prof)
+    got = run(ctx, m, pp, fp)
+    ref = orc.process(m, pp, fp, "f32")
+    assert not np.isnan(got).any()
+    assert np.all(got[..., 3] == 1.0)
+    tol = TOL_FP32[deb] if storage == L.STORAGE_FP32 else TOL_FP16
+    assert max_rel(got, ref) < tol, (max_rel(got, ref), max_abs(got, ref))
+    if storage == L.STORAGE_FP32:
+        assert max_rel(got, orc.process(m, pp, fp, "f64")) < 1e-3
+
+
+@pytest.mark.parametrize("impl", [L.IMPL_FUSED, L.IMPL_PLAIN])
+def test_full_chain_vs_oracle(ctx, impl):
+    """The single-frame chain of the headline workload at a small size:
+    VST + NLM 1.0 + RCD + ACES AP1 (with RGC) + AWB."""
+    w, h = 256, 160
+    c = W.config(2, w, h)
+    m = c.frame()
+    prof = W.make_profile()
+    pp = L.pipeline_params(w, h, debayer=c.debayer, out_space=c.out_space, flags=c.flags,
+                           out_format=L.FORMAT_RGBA32F, impl=impl)
+    fp = L.frame_params(prof, **c.frame_kwargs())
+    got = run(ctx, m, pp, fp)
+    ref = orc.process(m, pp, fp, "f32")
+    ref64 = orc.process(m, pp, fp, "f64")
+    assert max_rel(got, ref) < 2e-3, max_rel(got, ref)
+    assert max_rel(got, ref64) < 2e-3, max_rel(got, ref64)
+    assert psnr(got, ref64) > 70
+
+
+def test_denoise_mosaic_vs_oracle(ctx):
+    from gpu_util import download_image, upload_mosaic, alloc_rgba
+    w, h = 192, 128
+    m = frame(w, h, 31, a=8.0, b=80.0)
+    prof = W.make_profile()
+    model = W.noise_model(8.0, 80.0)
+    for strength in (0.5, 1.0, 2.0):
+        pp = L.pipeline_params(w, h, flags=L.FLAG_DENOISE | L.FLAG_KEEP_INTERMEDIATE,
+                               out_format=L.FORMAT_RGBA32F)
+        fp = L.frame_params(prof, denoise_strength=strength, noise_override=model)
+        with L.Pipeline(ctx, pp) as pipe:
+            _, src = upload_mosaic(m)
+            _, dst = alloc_rgba(w, h)
+            pipe.record(torch.cuda.current_stream().cuda_stream, src, dst, fp)
+            _, mos = pipe.intermediate()
+            got = download_image(mos, "r16")
+        ref, _ = orc.denoise_temporal(m, prof, model, strength, 0.0)
+        d = np.abs(got.astype(np.int32) - ref.astype(np.int32))
+        assert d.max() <= 1, (strength, d.max())
+        assert (d > 0).mean() < 0.01, (strength, (d > 0).mean())
+        # The filter did something.
+        assert np.abs(got.astype(np.int32) - m.astype(np.int32)).mean() > 0.5
+
+
+@pytest.mark.parametrize("storage", [L.STORAGE_FP32, L.STORAGE_FP16])
+@pytest.mark.parametrize("deb", [L.DEBAYER_BILINEAR, L.DEBAYER_RCD])
+@pytest.mark.parametrize("chroma", [False, True])
+def test_awb_bit_exact(ctx, deb, storage, chroma):
+    """The GPU histogram equals the CPU builder's on the intermediate the
+    GPU produced, in all three counters, bit for bit."""
+    from gpu_util import download_image
+    w, h = 320, 200
+    m = frame(w, h, 41 + deb)
+    prof = W.make_profile()
+    flags = L.FLAG_AWB_HISTOGRAM | L.FLAG_KEEP_INTERMEDIATE | (L.FLAG_CHROMA_DENOISE if chroma else 0)
+    pp = L.pipeline_params(w, h, debayer=deb, flags=flags, out_format=L.FORMAT_RGBA32F,
+                           storage=storage, nb_awb_slots=2)
+    fp = L.frame_params(prof, denoise_chroma_strength=0.5 if chroma else 0.0)
+    from gpu_util import upload_mosaic, alloc_rgba
+    with L.Pipeline(ctx, pp) as pipe:
+        _, src = upload_mosaic(m)
+        _, dst = alloc_rgba(w, h)
+        pipe.record(torch.cuda.current_stream().cuda_stream, src, dst, fp)
+        torch.cuda.synchronize()
+        rgb_img, _ = pipe.intermediate()
+        rgb = download_image(rgb_img, "rgba16f" if storage == L.STORAGE_FP16 else "rgba32f").astype(np.float32)
+        hist = pipe.awb_histogram()
+    cnt, wgt, brt = L.awb_histogram_from_rgb(rgb, W.WB)
+    assert cnt.sum() > 0.5 * (w // 8) * (h // 8)
+    assert np.array_equal(hist.count, cnt)
+    assert np.array_equal(hist.weight, wgt)
+    assert np.array_equal(hist.weight_bright, brt)
+    ocnt, _, _ = orc.awb_histogram(rgb, W.WB)
+    assert np.array_equal(ocnt, cnt)
+
+
+def test_chroma_vs_oracle(ctx):
+    w, h = 240, 160
+    c = W.config(3, w, h)
+    m = c.frame()
+    prof = W.make_profile()
+    pp = L.pipeline_params(w, h, debayer=L.DEBAYER_MHC, out_space=L.CS_P3D65,
+                           flags=L.FLAG_CHROMA_DENOISE, out_format=L.FORMAT_RGBA32F)
+    for s in (0.5, 1.0):
+        fp = L.frame_params(prof, denoise_chroma_strength=s)
+        got = run(ctx, m, pp, fp)
+        ref = orc.process(m, pp, fp, "f32")
+        assert max_rel(got, ref) < 2e-4, (s, max_rel(got, ref))
+
+
+def test_temporal_sequence_vs_oracle(ctx):
+    """Five frames with moving rectangles: temporal 0.8 + NLM 1.0; the
+    denoised mosaic, the state and the output follow the oracle's chain."""
+    from gpu_util import download_image, upload_mosaic, alloc_rgba
+    w, h = 160, 112
+    c = W.config(3, w, h)
+    prof = W.make_profile()
+    model = W.noise_model(c.noise_a_dn, c.noise_b_dn)
+    pp = L.pipeline_params(w, h, debayer=L.DEBAYER_MHC, out_space=L.CS_P3D65,
+                           flags=L.FLAG_DENOISE | L.FLAG_TEMPORAL_DENOISE | L.FLAG_KEEP_INTERMEDIATE,
+                           out_format=L.FORMAT_RGBA32F)
+    fp = L.frame_params(prof, denoise_strength=1.0, denoise_temporal_strength=0.8, noise_override=model)
+    prev = None
+    with L.Pipeline(ctx, pp) as pipe:
+        for f in range(5):
+            m = c.frame(f)
+            _, src = upload_mosaic(m)
+            _, dst = alloc_rgba(w, h)
+            pipe.record(torch.cuda.current_stream().cuda_stream, src, dst, fp)
+            _, mos = pipe.intermediate()
+            got = download_image(mos, "r16")
+            lvl, var = pipe.temporal_state()
+            glvl = download_image(lvl, "r32f")
+            gvar = download_image(var, "r8")
+            clean, nxt = orc.denoise_temporal(m, prof, model, 1.0, 0.8, prev)
+            d = np.abs(got.astype(np.int32) - clean.astype(np.int32))
+            assert d.max() <= 2 and (d > 0).mean() < 0.02, (f, d.max(), (d > 0).mean())
+            assert np.max(np.abs(glvl - nxt[0])) < 1e-4, f
+            qv = (gvar.astype(np.float32) / 255.0) ** 2
+            assert np.max(np.abs(qv - nxt[1])) < 0.01, f
+            # Follow the GPU's own state so the comparison does not drift.
+            prev = np.stack([glvl, qv]).astype(np.float32)
+
+
+def test_plain_and_fused_agree(ctx):
+    w, h = 256, 144
+    c = W.config(2, w, h)
+    m = c.frame()
+    prof = W.make_profile()
+    fp = L.frame_params(prof, **c.frame_kwargs())
+    outs = []
+    for impl in (L.IMPL_FUSED, L.IMPL_PLAIN):
+        pp = L.pipeline_params(w, h, debayer=c.debayer, out_space=c.out_space, flags=c.flags,
+                               out_format=L.FORMAT_RGBA32F, impl=impl)
+        outs.append(run(ctx, m, pp, fp))
+    assert max_rel(outs[0], outs[1]) < 2e-3
+
+
+def test_rgba16f_output(ctx):
+    w, h = 128, 96
+    m = frame(w, h, 51)
+    prof = W.make_profile()
+    pp = L.pipeline_params(w, h, debayer=L.DEBAYER_RCD, out_space=L.CS_BT2020,
+                           out_format=L.FORMAT_RGBA16F)
+    fp = L.frame_params(prof)
+    got = run(ctx, m, pp, fp, L.FORMAT_RGBA16F)
+    ref = orc.process(m, pp, fp, "f32")
+    assert max_rel(got, ref) < 3e-3
+
+
+def test_frame_options_vs_oracle(ctx):
+    """Rebalance to an illuminant, exposure, clamp, the output-space
+    override and the RGC veto."""
+    import golden.make_golden as MG
+    w, h = 128, 96
+    m = frame(w, h, 61)
+    prof = MG.golden_profile()
+    pp = L.pipeline_params(w, h, debayer=L.DEBAYER_MHC, out_space=L.CS_XYZ_D65,
+                           out_format=L.FORMAT_RGBA32F)
+    cases = [
+        dict(wb_mode=L.WB_REBALANCE, illuminant=(3200.0, 0.02)),
+        dict(exposure_stops=1.5, flags=L.FRAME_CLAMP_NEGATIVE),
+        dict(out_space=L.CS_ACES_AP1, out_space_set=True),
+        dict(out_space=L.CS_ACES_AP1, out_space_set=True, flags=L.FRAME_NO_GAMUT_COMPRESSION),
+        dict(out_space=L.CS_V_GAMUT, out_space_set=True),
+    ]
+    for kw in cases:
+        fp = L.frame_params(prof, **kw)
+        got = run(ctx, m, pp, fp)
+        ref = orc.process(m, pp, fp, "f32")
+        assert max_rel(got, ref) < 2e-4, (kw, max_rel(got, ref))
+
+
+@pytest.mark.parametrize("wh", [(8, 8), (16, 10), (24, 24), (62, 46), (1030, 18)])
+def test_edge_sizes(ctx, wh):
+    """Frames smaller than a tile or an apron, and ragged last tiles."""
+    w, h = wh
+    m = frame(w, h, 71)
+    prof = W.make_profile()
+    for deb in (0, 1, 2):
+        pp = L.pipeline_params(w, h, debayer=deb, out_space=L.CS_BT709, out_format=L.FORMAT_RGBA32F,
+                               flags=L.FLAG_AWB_HISTOGRAM)
+        fp = L.frame_params(prof)
+        got = run(ctx, m, pp, fp)
+        ref = orc.process(m, pp, fp, "f32")
+        assert max_rel(got, ref) < TOL_FP32[deb], (wh, deb, max_rel(got, ref))
+    if w >= 12 and h >= 12:
+        pp = L.pipeline_params(w, h, debayer=2, flags=L.FLAG_DENOISE, out_format=L.FORMAT_RGBA32F)
+        fp = L.frame_params(prof, denoise_strength=1.0, noise_override=W.noise_model(4, 40))
+        got = run(ctx, m, pp, fp)
+        assert max_rel(got, orc.process(m, pp, fp, "f32")) < 2e-3
