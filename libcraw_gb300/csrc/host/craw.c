@@ -56,6 +56,7 @@ CRAW_API int craw_cuda_check_device(int device, const char **missing)
         missing = &dummy;
     *missing = NULL;
     if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) {
+        (void)cudaGetLastError();
         *missing = "a CUDA device with that ordinal";
         return CRAW_ERROR(ENOTSUP);
     }

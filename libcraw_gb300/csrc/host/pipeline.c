@@ -477,6 +477,7 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
         }
         dk.black[s4] = fp->profile->black_level[s4];
         dk.range[s4] = range;
+        dk.inv_range[s4] = 1.0f / range;
         dk.wbs[s4] = frame.wb[chan[s4]];
     }
     for (int c = 0; c < 3; c++)

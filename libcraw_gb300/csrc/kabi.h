@@ -72,7 +72,7 @@ typedef struct CRAWKColor {
 
 typedef struct CRAWKDevelop {
     int32_t width, height;
-    float black[4], range[4], wbs[4];   /* per site; wbs = gain of the site's channel */
+    float black[4], range[4], inv_range[4], wbs[4];   /* per site; wbs = gain of the site's channel */
     float clip;                         /* 1.0 */
     int32_t method;                     /* CRAW_DEBAYER_* */
     int32_t fp16;                       /* intermediate values rounded to half */

@@ -58,6 +58,7 @@ k_awb_reduce(const uint64_t *__restrict__ rec, uint32_t n, uint32_t *__restrict_
 
 extern "C" int craw_k_awb_reduce(const uint64_t *rec, uint32_t n, uint32_t *hist, cudaStream_t s)
 {
+    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
     static bool attr_set = false;
     const int smem = 3 * kBins * (int)sizeof(uint32_t);
     if (!attr_set) {

@@ -136,6 +136,7 @@ k_chroma_up_color(const CRAWKDevelop k, const CRAWKChroma c, const void *inter, 
 extern "C" int craw_k_chroma_blur(const CRAWKChroma *c, const void *q, size_t q_pitch,
                                   void *qf, size_t qf_pitch, cudaStream_t s)
 {
+    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
     dim3 grid((c->qw + BX - 1) / BX, (c->qh + BY - 1) / BY);
     k_chroma_blur<<<grid, BX * BY, 0, s>>>(*c, q, q_pitch, qf, qf_pitch);
     return cudaGetLastError() == cudaSuccess ? 0 : -5;
@@ -147,6 +148,7 @@ extern "C" int craw_k_chroma_up_color(const CRAWKDevelop *k, const CRAWKChroma *
                                       void *dst, size_t dst_pitch, int dst_half,
                                       void *inter_out, const CRAWKAwbOut *awb, cudaStream_t s)
 {
+    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
     dim3 grid((c->width + TW - 1) / TW, (c->height + TH - 1) / TH);
     k_chroma_up_color<<<grid, NT, 0, s>>>(*k, *c, inter, inter_pitch, q, qf, q_pitch, dst,
                                           dst_pitch, dst_half, inter_out, *awb);

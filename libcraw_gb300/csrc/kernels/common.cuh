@@ -27,13 +27,11 @@ CRAW_DEV int craw_mirror(int v, int n)
 
 /* The prep of one raw sample at quad site s (reference
  * lib/ref/ref_debayer.c:42-63): UNORM, above black in units of the
- * site's range, times the gain of its channel, clipped. Division, not a
- * reciprocal, as the CPU reference divides. */
+ * site's range, times the gain of its channel, clipped at 1.0. */
 CRAW_DEV float craw_prep(const CRAWKDevelop &k, uint16_t raw, int s)
 {
     float r = (float)raw * (1.0f / 65535.0f);
-    float t = __fdiv_rn(__fsub_rn(r, k.black[s]), k.range[s]);
-    t = __fmul_rn(t, k.wbs[s]);
+    float t = (r - k.black[s]) * k.inv_range[s] * k.wbs[s];
     return t < k.clip ? t : k.clip;
 }
 
@@ -57,15 +55,15 @@ CRAW_DEV void craw_gamut_compress(const CRAWKColor &c, float o[3])
     float ach = fmaxf(o[0], fmaxf(o[1], o[2]));
     if (ach == 0.0f)
         return;
-    float mag = fabsf(ach);
+    float mag = fabsf(ach), inv_mag = 1.0f / mag;
 #pragma unroll
     for (int i = 0; i < 3; i++) {
-        float d = (ach - o[i]) / mag;
+        float d = (ach - o[i]) * inv_mag;
         if (d < c.gc_thr[i])
             continue;
         float nd = (d - c.gc_thr[i]) / c.gc_scl[i];
-        float p = powf(nd, c.gc_pwr);
-        d = c.gc_thr[i] + c.gc_scl[i] * nd / powf(1.0f + p, c.gc_inv_pwr);
+        float p = __powf(nd, c.gc_pwr);
+        d = c.gc_thr[i] + c.gc_scl[i] * nd * __powf(1.0f + p, -c.gc_inv_pwr);
         o[i] = ach - d * mag;
     }
 }
@@ -139,7 +137,11 @@ CRAW_DEV uint64_t craw_awb_block(float r, float g, float b, const float wb[3],
     y = y > lmin ? (y < lmax ? y : lmax) : lmin;
     float fx = __fmul_rn(__fdiv_rn(__fsub_rn(x, lmin), span), 128.0f);
     float fy = __fmul_rn(__fdiv_rn(__fsub_rn(y, lmin), span), 128.0f);
-    if (deferred && (fabsf(fx - rintf(fx)) < 2e-4f || fabsf(fy - rintf(fy)) < 2e-4f)) {
+    /* Edges at 0 and 128 cannot flip: the bin index is clamped there. */
+    const float rx = rintf(fx), ry = rintf(fy);
+    const bool near_x = rx >= 1.0f && rx <= 127.0f && fabsf(fx - rx) < 2e-4f;
+    const bool near_y = ry >= 1.0f && ry <= 127.0f && fabsf(fy - ry) < 2e-4f;
+    if (deferred && (near_x || near_y)) {
         uint32_t i = atomicAdd(nb_deferred, 1u);
         if (i < CRAW_K_AWB_DEFER_MAX) {
             CRAWKAwbDeferred d;

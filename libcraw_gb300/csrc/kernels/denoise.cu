@@ -79,6 +79,141 @@ struct Cfg {
     static constexpr int smem_floats = 4 * TN * (HISTORY ? 2 : 1) + (HISTORY ? 8 * EN : 0);
 };
 
+/* The NLM search of one thread: BW columns x M rows of one plane, at the
+ * tile position (ox0, oy0), over the 7x7 offsets (reference
+ * lib/ref/ref_denoise.c:109-154). Weights as exp2 on the MUFU:
+ * exp(-max(d2/(9h^2) - 2, 0)) = 2^min(d2 * c1 + c0, 0) with
+ * c1 = -log2(e)/(9h^2), c0 = 2 log2(e); with a history
+ * exp(-max(d2/(9h^2) - (vc + vq), 0) / vc) = 2^min((vc + vq - d2/(9h^2)) * log2(e)/vc, 0). */
+template <int BW, int M, int R, int TS, bool HISTORY>
+struct Search {
+    static_assert(BW % 2 == 0 && M % 2 == 0, "pairs of columns and rows");
+    float own[M + 2][BW + 2];
+    float acc[M][BW], wsum[M][BW];
+    float vc[HISTORY ? M : 1][BW], lvc[HISTORY ? M : 1][BW];
+    float kd, c1, c0;
+
+    CRAW_DEV void init(const float *Tp, const float *Vp, int ox0, int oy0, float inv_h2)
+    {
+#pragma unroll
+        for (int r = 0; r < M + 2; r++)
+#pragma unroll
+            for (int c = 0; c < BW + 2; c++)
+                own[r][c] = Tp[(oy0 + R - 1 + r) * TS + ox0 + R - 1 + c];
+        kd = (1.0f / 9.0f) * inv_h2;
+        c1 = -kLog2e * kd;
+        c0 = 2.0f * kLog2e;
+#pragma unroll
+        for (int m = 0; m < M; m++)
+#pragma unroll
+            for (int j = 0; j < BW; j++) {
+                acc[m][j] = 0.0f;
+                wsum[m][j] = 0.0f;
+                if constexpr (HISTORY) {
+                    vc[m][j] = Vp[(oy0 + R + m) * TS + ox0 + R + j];
+                    lvc[m][j] = __fdiv_rn(kLog2e, vc[m][j]);
+                }
+            }
+    }
+
+    /* One row of the shifted window: columns cs .. cs + BW + 1, where cs is
+     * even (ALIGNED) or odd; float2 loads either way. */
+    template <bool ALIGNED>
+    CRAW_DEV void load_row(const float *row, int cs, float w[BW + 2]) const
+    {
+        if constexpr (ALIGNED) {
+#pragma unroll
+            for (int c = 0; c < BW + 2; c += 2) {
+                float2 t = *reinterpret_cast<const float2 *>(row + cs + c);
+                w[c] = t.x;
+                w[c + 1] = t.y;
+            }
+        } else {
+            float2 t = *reinterpret_cast<const float2 *>(row + cs - 1);
+            w[0] = t.y;
+#pragma unroll
+            for (int c = 1; c < BW + 1; c += 2) {
+                float2 u = *reinterpret_cast<const float2 *>(row + cs + c);
+                w[c] = u.x;
+                w[c + 1] = u.y;
+            }
+            float2 v = *reinterpret_cast<const float2 *>(row + cs + BW + 1);
+            w[BW + 1] = v.x;
+        }
+    }
+
+    template <bool ALIGNED>
+    CRAW_DEV void step_dx(const float *Tp, const float *Vp, int ox0, int oy0, int dx)
+    {
+        const int cs = ox0 + R - 1 + dx;
+        float win[M + 2 + 2 * S][BW + 2];
+#pragma unroll
+        for (int rr = 0; rr < M + 2 + 2 * S; rr++)
+            load_row<ALIGNED>(Tp + (oy0 + R - 1 - S + rr) * TS, cs, win[rr]);
+        float vq[HISTORY ? M + 2 * S : 1][BW];
+        if constexpr (HISTORY) {
+            /* Columns cs + 1 .. cs + BW: aligned exactly when cs is odd. */
+#pragma unroll
+            for (int rr = 0; rr < M + 2 * S; rr++) {
+                const float *row = Vp + (oy0 + R - S + rr) * TS + cs + 1;
+                if constexpr (!ALIGNED) {
+#pragma unroll
+                    for (int j = 0; j < BW; j += 2) {
+                        float2 t = *reinterpret_cast<const float2 *>(row + j);
+                        vq[rr][j] = t.x;
+                        vq[rr][j + 1] = t.y;
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < BW; j++)
+                        vq[rr][j] = row[j];
+                }
+            }
+        }
+#pragma unroll
+        for (int dy = -S; dy <= S; dy++) {
+            float hs[M + 2][BW];
+#pragma unroll
+            for (int r = 0; r < M + 2; r++) {
+                float e[BW + 2];
+#pragma unroll
+                for (int c = 0; c < BW + 2; c++) {
+                    float d = own[r][c] - win[r + dy + S][c];
+                    e[c] = d * d;
+                }
+                /* Row sums of three, the middle pair shared by two columns. */
+#pragma unroll
+                for (int j = 0; j < BW; j += 2) {
+                    float mid = e[j + 1] + e[j + 2];
+                    hs[r][j] = e[j] + mid;
+                    hs[r][j + 1] = mid + e[j + 3];
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < M; m += 2) {
+#pragma unroll
+                for (int j = 0; j < BW; j++) {
+                    /* Column sums of three, the middle pair shared by two rows. */
+                    float mid = hs[m + 1][j] + hs[m + 2][j];
+                    float d2a = hs[m][j] + mid, d2b = mid + hs[m + 3][j];
+                    float wa, wb;
+                    if constexpr (HISTORY) {
+                        wa = craw_ex2(fminf(fmaf(d2a, -kd, vc[m][j] + vq[m + dy + S][j]) * lvc[m][j], 0.0f));
+                        wb = craw_ex2(fminf(fmaf(d2b, -kd, vc[m + 1][j] + vq[m + 1 + dy + S][j]) * lvc[m + 1][j], 0.0f));
+                    } else {
+                        wa = craw_ex2(fminf(fmaf(d2a, c1, c0), 0.0f));
+                        wb = craw_ex2(fminf(fmaf(d2b, c1, c0), 0.0f));
+                    }
+                    wsum[m][j] += wa;
+                    wsum[m + 1][j] += wb;
+                    acc[m][j] = fmaf(wa, win[m + 1 + dy + S][j + 1], acc[m][j]);
+                    acc[m + 1][j] = fmaf(wb, win[m + 2 + dy + S][j + 1], acc[m + 1][j]);
+                }
+            }
+        }
+    }
+};
+
 template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY>
 __global__ void __launch_bounds__(Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>::NT)
 k_denoise(const CRAWKDenoise k, const CRAWKDenoiseIO io)
@@ -161,100 +296,23 @@ k_denoise(const CRAWKDenoise k, const CRAWKDenoiseIO io)
 
     if constexpr (SPATIAL) {
         const float *Vp = V + pl * C::TN;
-        float own[M + 2][BW + 2];
-        float acc[M][BW], wsum[M][BW], vc[M][BW], lvc[M][BW];
-#pragma unroll
-        for (int r = 0; r < M + 2; r++)
-#pragma unroll
-            for (int c = 0; c < BW + 2; c++)
-                own[r][c] = Tp[(oy0 + R - 1 + r) * TS + ox0 + R - 1 + c];
-        const float kd = (1.0f / 9.0f) * k.inv_h2;   /* inv_np * inv_h2 */
-        const float c1 = -kLog2e * kd, c0 = 2.0f * kLog2e;
-#pragma unroll
-        for (int m = 0; m < M; m++)
-#pragma unroll
-            for (int j = 0; j < BW; j++) {
-                acc[m][j] = 0.0f;
-                wsum[m][j] = 0.0f;
-                if constexpr (HISTORY) {
-                    vc[m][j] = Vp[(oy0 + R + m) * TS + ox0 + R + j];
-                    lvc[m][j] = __fdiv_rn(kLog2e, vc[m][j]);
-                }
-            }
-
-#pragma unroll
-        for (int dx = -S; dx <= S; dx++) {
-            /* The shifted column block for this dx, every row any dy reads. */
-            float win[M + 2 + 2 * S][BW + 2];
-            const int cs = ox0 + R - 1 + dx;
-#pragma unroll
-            for (int rr = 0; rr < M + 2 + 2 * S; rr++) {
-                const float *row = Tp + (oy0 + R - 1 - S + rr) * TS;
-                if (((R - 1 + dx) & 1) == 0) {
-#pragma unroll
-                    for (int c = 0; c < BW + 2; c += 2) {
-                        float2 t = *reinterpret_cast<const float2 *>(row + cs + c);
-                        win[rr][c] = t.x;
-                        win[rr][c + 1] = t.y;
-                    }
-                } else {
-                    float2 t = *reinterpret_cast<const float2 *>(row + cs - 1);
-                    win[rr][0] = t.y;
-#pragma unroll
-                    for (int c = 1; c < BW + 1; c += 2) {
-                        float2 u = *reinterpret_cast<const float2 *>(row + cs + c);
-                        win[rr][c] = u.x;
-                        win[rr][c + 1] = u.y;
-                    }
-                    win[rr][BW + 1] = *(row + cs + BW + 1);
-                }
-            }
-            float vq[HISTORY ? M + 2 * S : 1][BW];
-            if constexpr (HISTORY) {
-#pragma unroll
-                for (int rr = 0; rr < M + 2 * S; rr++) {
-                    const float *row = Vp + (oy0 + R - S + rr) * TS + ox0 + R + dx;
-#pragma unroll
-                    for (int j = 0; j < BW; j++)
-                        vq[rr][j] = row[j];
-                }
-            }
-#pragma unroll
-            for (int dy = -S; dy <= S; dy++) {
-                float hs[M + 2][BW];
-#pragma unroll
-                for (int r = 0; r < M + 2; r++) {
-                    float e[BW + 2];
-#pragma unroll
-                    for (int c = 0; c < BW + 2; c++) {
-                        float d = own[r][c] - win[r + dy + S][c];
-                        e[c] = d * d;
-                    }
-#pragma unroll
-                    for (int j = 0; j < BW; j++)
-                        hs[r][j] = e[j] + e[j + 1] + e[j + 2];
-                }
-#pragma unroll
-                for (int m = 0; m < M; m++) {
-#pragma unroll
-                    for (int j = 0; j < BW; j++) {
-                        float d2 = hs[m][j] + hs[m + 1][j] + hs[m + 2][j];
-                        float w;
-                        if constexpr (HISTORY)
-                            w = craw_ex2(fminf(fmaf(d2, -kd, vc[m][j] + vq[m + dy + S][j]) * lvc[m][j], 0.0f));
-                        else
-                            w = craw_ex2(fminf(fmaf(d2, c1, c0), 0.0f));
-                        wsum[m][j] += w;
-                        acc[m][j] = fmaf(w, win[m + 1 + dy + S][j + 1], acc[m][j]);
-                    }
-                }
-            }
-        }
+        Search<BW, M, R, TS, HISTORY> st;
+        st.init(Tp, Vp, ox0, oy0, k.inv_h2);
+        /* dx is a runtime loop, in two groups by the alignment of the
+         * shifted window's first column, so that only the seven dy steps
+         * of one dx are unrolled and the code stays in the instruction
+         * cache. */
+#pragma unroll 1
+        for (int dx = -S; dx <= S; dx += 2)
+            st.template step_dx<((R - 1 - S) & 1) == 0>(Tp, Vp, ox0, oy0, dx);
+#pragma unroll 1
+        for (int dx = -S + 1; dx <= S - 1; dx += 2)
+            st.template step_dx<((R - S) & 1) == 0>(Tp, Vp, ox0, oy0, dx);
 #pragma unroll
         for (int m = 0; m < M; m++)
 #pragma unroll
             for (int j = 0; j < BW; j++)
-                res[m][j] = __fdiv_rn(acc[m][j], wsum[m][j]);
+                res[m][j] = __fdiv_rn(st.acc[m][j], st.wsum[m][j]);
     }
 
     /* ---- outputs: the next state, and the denoised mosaic in its raw
@@ -331,6 +389,7 @@ int dispatch(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, cudaStream_t s)
 extern "C" int craw_k_denoise(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, int shape,
                               cudaStream_t s)
 {
+    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
     switch (shape) {
     case CRAW_K_DN_SHAPE_2x8: return dispatch<2, 8, 1>(k, io, s);
     case CRAW_K_DN_SHAPE_2x4: return dispatch<2, 4, 2>(k, io, s);

@@ -45,17 +45,18 @@ template <int W, int H, int A, typename T> struct Tile {
 struct Frame {
     int x0, y0, w, h;
     bool interior;
+    template <bool INTERIOR>
     CRAW_DEV void map(int qx, int qy, int a, int tw, int th, int &px, int &py) const
     {
-        if (interior) {
+        if constexpr (INTERIOR) {
             px = qx;
             py = qy;
-            return;
+        } else {
+            px = craw_mirror(x0 + qx, w) - x0;
+            py = craw_mirror(y0 + qy, h) - y0;
+            px = px < -a ? -a : (px > tw - 1 + a ? tw - 1 + a : px);
+            py = py < -a ? -a : (py > th - 1 + a ? th - 1 + a : py);
         }
-        px = craw_mirror(x0 + qx, w) - x0;
-        py = craw_mirror(y0 + qy, h) - y0;
-        px = px < -a ? -a : (px > tw - 1 + a ? tw - 1 + a : px);
-        py = py < -a ? -a : (py > th - 1 + a ? th - 1 + a : py);
     }
 };
 
@@ -64,8 +65,11 @@ CRAW_DEV void load_prepped(const CRAWKDevelop &k, const CRAWKDevelopIO &io, cons
                            VT &v)
 {
     for (int i = threadIdx.x; i < VT::N; i += NT) {
-        int qx = i % VT::SX - A, qy = i / VT::SX - A;
-        int x = craw_mirror(f.x0 + qx, f.w), y = craw_mirror(f.y0 + qy, f.h);
+        int x = f.x0 + i % VT::SX - A, y = f.y0 + i / VT::SX - A;
+        if (!f.interior) {
+            x = craw_mirror(x, f.w);
+            y = craw_mirror(y, f.h);
+        }
         uint16_t raw = __ldg((const uint16_t *)((const char *)io.src + (size_t)y * io.src_pitch) + x);
         v.p[i] = craw_prep(k, raw, (y & 1) * 2 + (x & 1));
     }
@@ -128,7 +132,7 @@ CRAW_DEV float rcd_ratio(float a, float b)
 {
     a = fmaxf(a, 0.0f);
     b = fmaxf(b, 0.0f);
-    return __fdiv_rn(a - b, a + b + RCD_EPS);
+    return __fdividef(a - b, a + b + RCD_EPS);
 }
 
 /* The RCD passes of reference lib/ref/ref_debayer.c:204-395 on a tile,
@@ -156,12 +160,13 @@ struct RcdTile {
         c.p = base;
     }
 
+    template <bool IN>
     CRAW_DEV void run(const Frame &f)
     {
         /* Low pass, apron 4. */
         for (int i = threadIdx.x; i < decltype(l)::N; i += NT) {
             int px, py;
-            f.map(i % decltype(l)::SX - 4, i / decltype(l)::SX - 4, 4, TW, TH, px, py);
+            f.template map<IN>(i % decltype(l)::SX - 4, i / decltype(l)::SX - 4, 4, TW, TH, px, py);
 #define V(dx, dy) v.at(px + (dx), py + (dy))
             l.p[i] = (4.0f * V(0, 0) + 2.0f * (V(0, -1) + V(0, 1) + V(-1, 0) + V(1, 0))
                       + V(-1, -1) + V(1, -1) + V(-1, 1) + V(1, 1)) * (1.0f / 16.0f);
@@ -169,7 +174,7 @@ struct RcdTile {
         /* Vertical, horizontal and the two diagonal discriminations, apron 3. */
         for (int i = threadIdx.x; i < decltype(d)::N; i += NT) {
             int px, py;
-            f.map(i % decltype(d)::SX - 3, i / decltype(d)::SX - 3, 3, TW, TH, px, py);
+            f.template map<IN>(i % decltype(d)::SX - 3, i / decltype(d)::SX - 3, 3, TW, TH, px, py);
             float c2 = 2.0f * V(0, 0);
             float4 r;
             r.x = fabsf(V(0, -1) - V(0, 1)) + fabsf(c2 - V(0, -2) - V(0, 2));
@@ -182,7 +187,7 @@ struct RcdTile {
         /* Weights from 3x3 means of the discriminations, apron 2. */
         for (int i = threadIdx.x; i < decltype(w)::N; i += NT) {
             int px, py;
-            f.map(i % decltype(w)::SX - 2, i / decltype(w)::SX - 2, 2, TW, TH, px, py);
+            f.template map<IN>(i % decltype(w)::SX - 2, i / decltype(w)::SX - 2, 2, TW, TH, px, py);
             float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
             for (int dy = -1; dy <= 1; dy++)
@@ -193,13 +198,13 @@ struct RcdTile {
                 }
             float vs = s.x * (1.0f / 9.0f), hs = s.y * (1.0f / 9.0f);
             float ps = s.z * (1.0f / 9.0f), qs = s.w * (1.0f / 9.0f);
-            w.p[i] = make_float2(__fdiv_rn(hs, hs + vs + RCD_EPS), __fdiv_rn(qs, ps + qs + RCD_EPS));
+            w.p[i] = make_float2(__fdividef(hs, hs + vs + RCD_EPS), __fdividef(qs, ps + qs + RCD_EPS));
         }
         __syncthreads();
         /* Green at the R and B sites, apron 2. */
         for (int i = threadIdx.x; i < decltype(g)::N; i += NT) {
             int px, py;
-            f.map(i % decltype(g)::SX - 2, i / decltype(g)::SX - 2, 2, TW, TH, px, py);
+            f.template map<IN>(i % decltype(g)::SX - 2, i / decltype(g)::SX - 2, 2, TW, TH, px, py);
             int s = ((f.y0 + py) & 1) * 2 + ((f.x0 + px) & 1);
             if (s == 1 || s == 2) {
                 g.p[i] = V(0, 0);
@@ -219,7 +224,7 @@ struct RcdTile {
         /* The missing colour at the R and B sites, apron 1. */
         for (int i = threadIdx.x; i < decltype(c)::N; i += NT) {
             int px, py;
-            f.map(i % decltype(c)::SX - 1, i / decltype(c)::SX - 1, 1, TW, TH, px, py);
+            f.template map<IN>(i % decltype(c)::SX - 1, i / decltype(c)::SX - 1, 1, TW, TH, px, py);
             int s = ((f.y0 + py) & 1) * 2 + ((f.x0 + px) & 1);
             if (s == 1 || s == 2)
                 continue;
@@ -291,7 +296,10 @@ k_develop(const CRAWKDevelop k, const CRAWKDevelopIO io)
         t.carve(smem);
         load_prepped<TW, TH, NT, 5>(k, io, f, t.v);
         __syncthreads();
-        t.run(f);
+        if (f.interior)
+            t.template run<true>(f);
+        else
+            t.template run<false>(f);
 #pragma unroll
         for (int j = 0; j < PPT; j++) {
             int i = threadIdx.x + j * NT, x = i % TW, y = i / TW;
@@ -405,6 +413,7 @@ int launch(const CRAWKDevelop *k, const CRAWKDevelopIO *io, cudaStream_t s)
 extern "C" int craw_k_develop(const CRAWKDevelop *k, const CRAWKDevelopIO *io, int shape,
                               cudaStream_t s)
 {
+    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
     (void)shape;
     switch (k->method) {
     case kBilinear: return launch<kBilinear, 64, 16, 256>(k, io, s);

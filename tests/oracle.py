@@ -201,6 +201,30 @@ def max_rel(test: np.ndarray, ref: np.ndarray) -> float:
     return float(np.max(np.abs(t - r) / scale))
 
 
+def rel_map(test: np.ndarray, ref: np.ndarray) -> np.ndarray:
+    """The per-pixel error of max_rel()."""
+    t = test[..., :3].astype(np.float64)
+    r = ref[..., :3].astype(np.float64)
+    a = np.abs(r)
+    floor = max(1e-9, 0.01 * float(a.max()))
+    scale = np.maximum(a.max(axis=-1), floor)
+    return np.abs(t - r).max(axis=-1) / scale
+
+
+def denoised_chain_ok(test: np.ndarray, ref: np.ndarray) -> tuple[bool, dict]:
+    """The bound for a chain that includes the denoise. Its output mosaic
+    is re-encoded to 16-bit codes (reference lib/ref/ref_denoise.c:318-323),
+    so any two float evaluations differ by one code at the samples whose
+    value lies within rounding of a code boundary -- the reference's own
+    float code does against its double run (tests/test_oracle_pin.py) --
+    and a one-code step is up to ~1e-2 of a dark pixel. Bound: max_rel
+    under 1.5e-2, at most 0.1% of pixels above 1e-3, PSNR above 80 dB."""
+    r = rel_map(test, ref)
+    st = {"max_rel": float(r.max()), "frac_over_1e-3": float((r > 1e-3).mean()),
+          "psnr": psnr(test, ref)}
+    return (st["max_rel"] < 1.5e-2 and st["frac_over_1e-3"] < 1e-3 and st["psnr"] > 80), st
+
+
 def psnr(test: np.ndarray, ref: np.ndarray) -> float:
     t = test[..., :3].astype(np.float64)
     r = ref[..., :3].astype(np.float64)

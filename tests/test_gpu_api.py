@@ -35,7 +35,7 @@ def test_create_errors(ctx):
         dict(width=7, height=8), dict(width=6, height=8), dict(width=0, height=8),
         dict(width=64, height=48, out_format=L.FORMAT_R16_UNORM),
         dict(width=64, height=48, debayer=3), dict(width=64, height=48, out_space=9),
-        dict(width=10, height=10, flags=L.FLAG_DENOISE),
+        dict(width=8, height=8, flags=L.FLAG_DENOISE),
         dict(width=10, height=12, flags=L.FLAG_TEMPORAL_DENOISE),
     ]
     for kw in bad:
