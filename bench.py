@@ -394,9 +394,9 @@ def run_gpu(args):
             "stage_ms": {k: statistics.mean(v) for k, v in stage.items()},
             "roofline": roof, "roofline_fp32": roof32,
             "e2e": e2e,
-            # Our kernels per step: fused = denoise, develop, awb_reduce; plain =
-            # vst + nlm, prep + 8 RCD sweeps + awb + colour.
-            "gpu_launches": args.steps * (3 if impl == L.IMPL_FUSED else 13),
+            # Our kernels per step: fused = denoise, RCD quad tiles, RCD border
+            # tiles, awb_reduce; plain = vst + nlm, prep + 8 RCD sweeps + awb + colour.
+            "gpu_launches": args.steps * (4 if impl == L.IMPL_FUSED else 13),
             "clocks": {k: clk_s[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
             "awb_samples": int(hist.count.sum()),
             "wall_s_timed": wall,

@@ -13,10 +13,11 @@
  * The search: a thread owns BW columns x M rows of one plane. For a
  * search offset (dx, dy) it forms the squared differences of its own
  * (BW+2) x (M+2) window against the shifted one, sums them along x and
- * then along y in registers, and turns each of its BW*M patch distances
- * into a weight with one ex2 on the MUFU. The shifted windows of one dx
- * share all but one row between consecutive dy, so a column of the tile
- * is read from shared memory once per dx for all seven dy.
+ * then along y in registers (sharing the middle pair of each three-sum),
+ * and turns each of its BW*M patch distances into a weight with one ex2
+ * on the MUFU. For one dy the shifted rows of all seven dx are a single
+ * register block, read from shared memory once; dy is a runtime loop so
+ * that the unrolled body of seven dx stays in the instruction cache.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -42,6 +43,11 @@ CRAW_DEV float gat_inv(const CRAWKDenoise &k, float t)
     if (t >= k.gat_t0)
         return k.gat_inv * t * t - k.gat_off;
     return (t - k.gat_t0) * k.gat_sc;
+}
+
+CRAW_DEV float pick4(const float a[4], int i)
+{
+    return i == 0 ? a[0] : (i == 1 ? a[1] : (i == 2 ? a[2] : a[3]));
 }
 
 CRAW_DEV float level(const CRAWKDenoise &k, uint32_t raw, int pl)
@@ -116,69 +122,49 @@ struct Search {
             }
     }
 
-    /* One row of the shifted window: columns cs .. cs + BW + 1, where cs is
-     * even (ALIGNED) or odd; float2 loads either way. */
-    template <bool ALIGNED>
-    CRAW_DEV void load_row(const float *row, int cs, float w[BW + 2]) const
+    /* All seven dx of one dy. The shifted rows of this dy, every column any
+     * dx reads, are one register block: rows oy0 + R - 1 + dy .. + M + 1,
+     * columns ox0 .. ox0 + BW + 2S + 1 (ox0 is even and R - 1 = S, so every
+     * float2 load is aligned), read once from shared memory for seven dx. */
+    CRAW_DEV void step_dy(const float *Tp, const float *Vp, int ox0, int oy0, int dy)
     {
-        if constexpr (ALIGNED) {
+        constexpr int WC = BW + 2 + 2 * S;
+        static_assert(R - 1 == S, "window origin");
+        float win[M + 2][WC];
 #pragma unroll
-            for (int c = 0; c < BW + 2; c += 2) {
-                float2 t = *reinterpret_cast<const float2 *>(row + cs + c);
-                w[c] = t.x;
-                w[c + 1] = t.y;
-            }
-        } else {
-            float2 t = *reinterpret_cast<const float2 *>(row + cs - 1);
-            w[0] = t.y;
+        for (int r = 0; r < M + 2; r++) {
+            const float *row = Tp + (oy0 + R - 1 + dy + r) * TS + ox0;
 #pragma unroll
-            for (int c = 1; c < BW + 1; c += 2) {
-                float2 u = *reinterpret_cast<const float2 *>(row + cs + c);
-                w[c] = u.x;
-                w[c + 1] = u.y;
+            for (int c = 0; c < WC; c += 2) {
+                float2 t = *reinterpret_cast<const float2 *>(row + c);
+                win[r][c] = t.x;
+                win[r][c + 1] = t.y;
             }
-            float2 v = *reinterpret_cast<const float2 *>(row + cs + BW + 1);
-            w[BW + 1] = v.x;
         }
-    }
-
-    template <bool ALIGNED>
-    CRAW_DEV void step_dx(const float *Tp, const float *Vp, int ox0, int oy0, int dx)
-    {
-        const int cs = ox0 + R - 1 + dx;
-        float win[M + 2 + 2 * S][BW + 2];
-#pragma unroll
-        for (int rr = 0; rr < M + 2 + 2 * S; rr++)
-            load_row<ALIGNED>(Tp + (oy0 + R - 1 - S + rr) * TS, cs, win[rr]);
-        float vq[HISTORY ? M + 2 * S : 1][BW];
+        /* History: the variance of the shifted centres, columns
+         * ox0 + 1 .. ox0 + BW + 2S (loaded from ox0 in pairs). */
+        float vq[HISTORY ? M : 1][HISTORY ? BW + 2 * S + 2 : 1];
         if constexpr (HISTORY) {
-            /* Columns cs + 1 .. cs + BW: aligned exactly when cs is odd. */
 #pragma unroll
-            for (int rr = 0; rr < M + 2 * S; rr++) {
-                const float *row = Vp + (oy0 + R - S + rr) * TS + cs + 1;
-                if constexpr (!ALIGNED) {
+            for (int m = 0; m < M; m++) {
+                const float *row = Vp + (oy0 + R + dy + m) * TS + ox0;
 #pragma unroll
-                    for (int j = 0; j < BW; j += 2) {
-                        float2 t = *reinterpret_cast<const float2 *>(row + j);
-                        vq[rr][j] = t.x;
-                        vq[rr][j + 1] = t.y;
-                    }
-                } else {
-#pragma unroll
-                    for (int j = 0; j < BW; j++)
-                        vq[rr][j] = row[j];
+                for (int c = 0; c < BW + 2 * S + 2; c += 2) {
+                    float2 t = *reinterpret_cast<const float2 *>(row + c);
+                    vq[m][c] = t.x;
+                    vq[m][c + 1] = t.y;
                 }
             }
         }
 #pragma unroll
-        for (int dy = -S; dy <= S; dy++) {
+        for (int dx = -S; dx <= S; dx++) {
             float hs[M + 2][BW];
 #pragma unroll
             for (int r = 0; r < M + 2; r++) {
                 float e[BW + 2];
 #pragma unroll
                 for (int c = 0; c < BW + 2; c++) {
-                    float d = own[r][c] - win[r + dy + S][c];
+                    float d = own[r][c] - win[r][c + dx + S];
                     e[c] = d * d;
                 }
                 /* Row sums of three, the middle pair shared by two columns. */
@@ -198,16 +184,16 @@ struct Search {
                     float d2a = hs[m][j] + mid, d2b = mid + hs[m + 3][j];
                     float wa, wb;
                     if constexpr (HISTORY) {
-                        wa = craw_ex2(fminf(fmaf(d2a, -kd, vc[m][j] + vq[m + dy + S][j]) * lvc[m][j], 0.0f));
-                        wb = craw_ex2(fminf(fmaf(d2b, -kd, vc[m + 1][j] + vq[m + 1 + dy + S][j]) * lvc[m + 1][j], 0.0f));
+                        wa = craw_ex2(fminf(fmaf(d2a, -kd, vc[m][j] + vq[m][j + 1 + dx + S]) * lvc[m][j], 0.0f));
+                        wb = craw_ex2(fminf(fmaf(d2b, -kd, vc[m + 1][j] + vq[m + 1][j + 1 + dx + S]) * lvc[m + 1][j], 0.0f));
                     } else {
                         wa = craw_ex2(fminf(fmaf(d2a, c1, c0), 0.0f));
                         wb = craw_ex2(fminf(fmaf(d2b, c1, c0), 0.0f));
                     }
                     wsum[m][j] += wa;
                     wsum[m + 1][j] += wb;
-                    acc[m][j] = fmaf(wa, win[m + 1 + dy + S][j + 1], acc[m][j]);
-                    acc[m + 1][j] = fmaf(wb, win[m + 2 + dy + S][j + 1], acc[m + 1][j]);
+                    acc[m][j] = fmaf(wa, win[m + 1][j + 1 + dx + S], acc[m][j]);
+                    acc[m + 1][j] = fmaf(wb, win[m + 2][j + 1 + dx + S], acc[m + 1][j]);
                 }
             }
         }
@@ -298,16 +284,11 @@ k_denoise(const CRAWKDenoise k, const CRAWKDenoiseIO io)
         const float *Vp = V + pl * C::TN;
         Search<BW, M, R, TS, HISTORY> st;
         st.init(Tp, Vp, ox0, oy0, k.inv_h2);
-        /* dx is a runtime loop, in two groups by the alignment of the
-         * shifted window's first column, so that only the seven dy steps
-         * of one dx are unrolled and the code stays in the instruction
-         * cache. */
+        /* dy is a runtime loop and only the seven dx of one dy are
+         * unrolled, so that the loop body stays in the instruction cache. */
 #pragma unroll 1
-        for (int dx = -S; dx <= S; dx += 2)
-            st.template step_dx<((R - 1 - S) & 1) == 0>(Tp, Vp, ox0, oy0, dx);
-#pragma unroll 1
-        for (int dx = -S + 1; dx <= S - 1; dx += 2)
-            st.template step_dx<((R - S) & 1) == 0>(Tp, Vp, ox0, oy0, dx);
+        for (int dy = -S; dy <= S; dy++)
+            st.step_dy(Tp, Vp, ox0, oy0, dy);
 #pragma unroll
         for (int m = 0; m < M; m++)
 #pragma unroll
@@ -319,15 +300,16 @@ k_denoise(const CRAWKDenoise k, const CRAWKDenoiseIO io)
      * encoding after the highlight guard (reference
      * lib/ref/ref_denoise.c:285-324). */
     const int px = pl & 1, py = pl >> 1;
+    /* This warp's plane constants, selected once (indexing the parameter
+     * arrays with the warp's plane would copy them to local memory). */
+    const float blk = pick4(k.black, pl), irng = pick4(k.inv_range, pl), rng = pick4(k.range, pl);
 #pragma unroll
     for (int m = 0; m < M; m++) {
         const int qy = ty0 + oy0 + m;
-        if (qy >= k.ph)
-            break;
 #pragma unroll
         for (int j = 0; j < BW; j++) {
             const int qx = tx0 + ox0 + j;
-            if (qx >= k.pw)
+            if (qy >= k.ph || qx >= k.pw)
                 continue;
             const int my = 2 * qy + py, mx = 2 * qx + px;
             const float tc = Tp[(oy0 + R + m) * TS + ox0 + R + j];
@@ -344,10 +326,10 @@ k_denoise(const CRAWKDenoise k, const CRAWKDenoiseIO io)
             }
             float u = gat_inv(k, SPATIAL ? res[m][j] : tc);
             uint16_t raw0 = __ldg((const uint16_t *)((const char *)io.src + (size_t)my * io.src_pitch) + mx);
-            float u0 = level(k, raw0, pl);
+            float u0 = ((float)raw0 * (1.0f / 65535.0f) - blk) * irng;
             float gr = fminf(fmaxf((u0 - k.guard_lo) * k.guard_inv, 0.0f), 1.0f);
             u = u + (u0 - u) * gr;
-            float ro = fminf(fmaxf(k.black[pl] + u * k.range[pl], 0.0f), 1.0f);
+            float ro = fminf(fmaxf(blk + u * rng, 0.0f), 1.0f);
             uint16_t *dr = (uint16_t *)((char *)io.dst + (size_t)my * io.dst_pitch);
             dr[mx] = (uint16_t)rintf(ro * 65535.0f);
         }

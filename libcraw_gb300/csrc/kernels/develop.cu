@@ -264,15 +264,348 @@ struct RcdTile {
     }
 };
 
-/* ------------------------------------------------------------- kernel */
+/* ------------------------------------------------------- RCD, by quads */
 
-template <int METHOD, int TW, int TH, int NT> struct DevelopSmem {
+/* The RCD of an interior tile (all aprons inside the frame), one thread
+ * per 2x2 CFA quad (R at (0,0), Gr (1,0), Gb (0,1), B (1,1)): the site of
+ * every value is static, the neighbours a quad's four sites share are
+ * read once, and shared memory moves in float2 and float4. Same passes,
+ * same formulas as the per-pixel version above; the only arithmetic
+ * difference is the order of the 3x3 sums of the discriminations, taken
+ * here as rows of three and then three rows.
+ *
+ * Arrays (tile-relative pixel or quad coordinates, their ranges):
+ *   Vp float   pixels [-6, TW+6) x [-6, TH+6)   the prepped mosaic
+ *   Lq float2  quads  [-2, QW+2) x [-2, QH+2)   low pass at R and at B
+ *   Dp float4  pixels [-4, TW+4) x [-4, TH+4)   (V, H, P, Q) discriminations
+ *   Wp float2  pixels [-2, TW+2) x [-2, TH+2)   (wv, wp) weights
+ *   Gq float2  quads  [-1, QW+1) x [-1, QH+1)   green at R and at B
+ *   Cq float2  quads  [-1, QW+1) x [-1, QH+1)   B at R, R at B
+ * Gq, Cq and the output planes reuse Dp's space once the weights exist. */
+template <int TW, int TH, int NT>
+struct RcdQuads {
+    static constexpr int QW = TW / 2, QH = TH / 2;
+    static constexpr int VS = TW + 12, DS = TW + 8, WS = TW + 4, LS = QW + 4, GS = QW + 2;
+    static constexpr int VN = (TH + 12) * VS, DN = (TH + 8) * DS, WN = (TH + 4) * WS;
+    static constexpr int LN = (QH + 4) * LS, GN = (QH + 2) * GS;
+    static constexpr int floats = 4 * DN + 2 * WN + 2 * LN + VN;
+    static_assert(2 * GN * 2 + 3 * TW * TH <= 4 * DN, "G, C and the output fit in D's space");
+
+    float4 *Dp;
+    float2 *Wp, *Lq, *Gq, *Cq;
+    float *Vp;
+    float *rgb;   /* planar R, G, B of the tile */
+
+    CRAW_DEV void carve(float *base)
+    {
+        Dp = reinterpret_cast<float4 *>(base);
+        Wp = reinterpret_cast<float2 *>(base + 4 * DN);
+        Lq = reinterpret_cast<float2 *>(base + 4 * DN + 2 * WN);
+        Vp = base + 4 * DN + 2 * WN + 2 * LN;
+        Gq = reinterpret_cast<float2 *>(base);
+        Cq = reinterpret_cast<float2 *>(base + 2 * GN);
+        rgb = base + 4 * GN;
+    }
+
+    CRAW_DEV float V(int x, int y) const { return Vp[(y + 6) * VS + x + 6]; }
+    CRAW_DEV float2 V2(int x, int y) const
+    {
+        return *reinterpret_cast<const float2 *>(&Vp[(y + 6) * VS + x + 6]);
+    }
+    CRAW_DEV float4 &D(int x, int y) const { return Dp[(y + 4) * DS + x + 4]; }
+    CRAW_DEV float2 &W(int x, int y) const { return Wp[(y + 2) * WS + x + 2]; }
+    CRAW_DEV float2 &Lat(int qx, int qy) const { return Lq[(qy + 2) * LS + qx + 2]; }
+    CRAW_DEV float2 &G(int qx, int qy) const { return Gq[(qy + 1) * GS + qx + 1]; }
+    CRAW_DEV float2 &Cat(int qx, int qy) const { return Cq[(qy + 1) * GS + qx + 1]; }
+
+    /* The prepped mosaic of the tile and its apron: two u32 (two samples
+     * each) per quad. */
+    CRAW_DEV void load(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, int y0)
+    {
+        constexpr int QX = QW + 6, QY = QH + 6;
+        for (int i = threadIdx.x; i < QX * QY; i += NT) {
+            int qx = i % QX - 3, qy = i / QX - 3;
+            int x = x0 + 2 * qx, y = y0 + 2 * qy;
+            const char *r0 = (const char *)io.src + (size_t)y * io.src_pitch;
+            uint32_t a = __ldg(reinterpret_cast<const uint32_t *>(r0) + x / 2);
+            uint32_t b = __ldg(reinterpret_cast<const uint32_t *>(r0 + io.src_pitch) + x / 2);
+            float2 top = make_float2(craw_prep(k, (uint16_t)(a & 0xffff), 0), craw_prep(k, (uint16_t)(a >> 16), 1));
+            float2 bot = make_float2(craw_prep(k, (uint16_t)(b & 0xffff), 2), craw_prep(k, (uint16_t)(b >> 16), 3));
+            *reinterpret_cast<float2 *>(&Vp[(2 * qy + 6) * VS + 2 * qx + 6]) = top;
+            *reinterpret_cast<float2 *>(&Vp[(2 * qy + 7) * VS + 2 * qx + 6]) = bot;
+        }
+    }
+
+    CRAW_DEV void run()
+    {
+        /* Low pass at R and B, and the four discriminations at every
+         * pixel, from the 6x6 window around the quad. */
+        for (int i = threadIdx.x; i < (QW + 4) * (QH + 4); i += NT) {
+            const int qx = i % (QW + 4) - 2, qy = i / (QW + 4) - 2;
+            float v[6][6];
+#pragma unroll
+            for (int r = 0; r < 6; r++)
+#pragma unroll
+                for (int c = 0; c < 6; c += 2) {
+                    float2 t = V2(2 * qx - 2 + c, 2 * qy - 2 + r);
+                    v[r][c] = t.x;
+                    v[r][c + 1] = t.y;
+                }
+            float lo[2];
+#pragma unroll
+            for (int s = 0; s < 2; s++) {
+                const int cy = 2 + s, cx = 2 + s;
+                lo[s] = (4.0f * v[cy][cx] + 2.0f * (v[cy - 1][cx] + v[cy + 1][cx] + v[cy][cx - 1] + v[cy][cx + 1])
+                         + v[cy - 1][cx - 1] + v[cy - 1][cx + 1] + v[cy + 1][cx - 1] + v[cy + 1][cx + 1]) * (1.0f / 16.0f);
+            }
+            Lat(qx, qy) = make_float2(lo[0], lo[1]);
+#pragma unroll
+            for (int b = 0; b < 2; b++)
+#pragma unroll
+                for (int a = 0; a < 2; a++) {
+                    const int cy = 2 + b, cx = 2 + a;
+                    float c2 = 2.0f * v[cy][cx];
+                    float4 d;
+                    d.x = fabsf(v[cy - 1][cx] - v[cy + 1][cx]) + fabsf(c2 - v[cy - 2][cx] - v[cy + 2][cx]);
+                    d.y = fabsf(v[cy][cx - 1] - v[cy][cx + 1]) + fabsf(c2 - v[cy][cx - 2] - v[cy][cx + 2]);
+                    d.z = fabsf(v[cy + 1][cx - 1] - v[cy - 1][cx + 1]) + fabsf(c2 - v[cy + 2][cx - 2] - v[cy - 2][cx + 2]);
+                    d.w = fabsf(v[cy - 1][cx - 1] - v[cy + 1][cx + 1]) + fabsf(c2 - v[cy - 2][cx - 2] - v[cy + 2][cx + 2]);
+                    D(2 * qx + a, 2 * qy + b) = d;
+                }
+        }
+        __syncthreads();
+        /* Weights: 3x3 means of the discriminations, as three-wide row sums
+         * of a 4x4 window and then three of those rows. */
+        for (int i = threadIdx.x; i < (QW + 2) * (QH + 2); i += NT) {
+            const int qx = i % (QW + 2) - 1, qy = i / (QW + 2) - 1;
+            float4 h[4][2];
+#pragma unroll
+            for (int r = 0; r < 4; r++) {
+                float4 d0 = D(2 * qx - 1, 2 * qy - 1 + r), d1 = D(2 * qx, 2 * qy - 1 + r);
+                float4 d2 = D(2 * qx + 1, 2 * qy - 1 + r), d3 = D(2 * qx + 2, 2 * qy - 1 + r);
+                float4 mid = make_float4(d1.x + d2.x, d1.y + d2.y, d1.z + d2.z, d1.w + d2.w);
+                h[r][0] = make_float4(d0.x + mid.x, d0.y + mid.y, d0.z + mid.z, d0.w + mid.w);
+                h[r][1] = make_float4(mid.x + d3.x, mid.y + d3.y, mid.z + d3.z, mid.w + d3.w);
+            }
+#pragma unroll
+            for (int a = 0; a < 2; a++) {
+                float4 mid = make_float4(h[1][a].x + h[2][a].x, h[1][a].y + h[2][a].y,
+                                         h[1][a].z + h[2][a].z, h[1][a].w + h[2][a].w);
+#pragma unroll
+                for (int b = 0; b < 2; b++) {
+                    float4 o = b == 0 ? h[0][a] : h[3][a];
+                    float vs = (o.x + mid.x) * (1.0f / 9.0f), hs = (o.y + mid.y) * (1.0f / 9.0f);
+                    float ps = (o.z + mid.z) * (1.0f / 9.0f), qs = (o.w + mid.w) * (1.0f / 9.0f);
+                    W(2 * qx + a, 2 * qy + b) = make_float2(__fdividef(hs, hs + vs + RCD_EPS),
+                                                            __fdividef(qs, ps + qs + RCD_EPS));
+                }
+            }
+        }
+        __syncthreads();
+        /* Green at R and at B (Gq lives where Dp was: D is dead now). */
+        for (int i = threadIdx.x; i < (QW + 2) * (QH + 2); i += NT) {
+            const int qx = i % (QW + 2) - 1, qy = i / (QW + 2) - 1;
+            const int x = 2 * qx, y = 2 * qy;
+            float2 l0 = Lat(qx, qy), lu = Lat(qx, qy - 1), ld = Lat(qx, qy + 1);
+            float2 ll = Lat(qx - 1, qy), lr = Lat(qx + 1, qy);
+            float gv = 0.5f * (V(x, y - 1) * (1.0f + rcd_ratio(l0.x, lu.x)) + V(x, y + 1) * (1.0f + rcd_ratio(l0.x, ld.x)));
+            float gh = 0.5f * (V(x - 1, y) * (1.0f + rcd_ratio(l0.x, ll.x)) + V(x + 1, y) * (1.0f + rcd_ratio(l0.x, lr.x)));
+            float w0 = W(x, y).x;
+            float g_r = w0 * gv + (1.0f - w0) * gh;
+            gv = 0.5f * (V(x + 1, y) * (1.0f + rcd_ratio(l0.y, lu.y)) + V(x + 1, y + 2) * (1.0f + rcd_ratio(l0.y, ld.y)));
+            gh = 0.5f * (V(x, y + 1) * (1.0f + rcd_ratio(l0.y, ll.y)) + V(x + 2, y + 1) * (1.0f + rcd_ratio(l0.y, lr.y)));
+            float w1 = W(x + 1, y + 1).x;
+            G(qx, qy) = make_float2(g_r, w1 * gv + (1.0f - w1) * gh);
+        }
+        __syncthreads();
+        /* The missing colour at R (from the B diagonals) and at B (from the
+         * R diagonals); each only where a later pass reads it. */
+        for (int i = threadIdx.x; i < (QW + 2) * (QH + 2); i += NT) {
+            const int qx = i % (QW + 2) - 1, qy = i / (QW + 2) - 1;
+            const int x = 2 * qx, y = 2 * qy;
+            float c_r = 0.0f, c_b = 0.0f;
+            if (qx >= 0 && qy >= 0) {
+                float g00 = G(qx, qy).x, wt = W(x, y).y;
+                float dsw = V(x - 1, y + 1) - G(qx - 1, qy).y, dne = V(x + 1, y - 1) - G(qx, qy - 1).y;
+                float dnw = V(x - 1, y - 1) - G(qx - 1, qy - 1).y, dse = V(x + 1, y + 1) - G(qx, qy).y;
+                c_r = wt * (g00 + 0.5f * (dsw + dne)) + (1.0f - wt) * (g00 + 0.5f * (dnw + dse));
+            }
+            if (qx < QW && qy < QH) {
+                float g00 = G(qx, qy).y, wt = W(x + 1, y + 1).y;
+                float dsw = V(x, y + 2) - G(qx, qy + 1).x, dne = V(x + 2, y) - G(qx + 1, qy).x;
+                float dnw = V(x, y) - G(qx, qy).x, dse = V(x + 2, y + 2) - G(qx + 1, qy + 1).x;
+                c_b = wt * (g00 + 0.5f * (dsw + dne)) + (1.0f - wt) * (g00 + 0.5f * (dnw + dse));
+            }
+            Cat(qx, qy) = make_float2(c_r, c_b);
+        }
+        __syncthreads();
+        /* The four output pixels of each quad, into the planar output. */
+        constexpr int P = TW * TH;
+        for (int i = threadIdx.x; i < QW * QH; i += NT) {
+            const int qx = i % QW, qy = i / QW, x = 2 * qx, y = 2 * qy;
+            float2 g0 = G(qx, qy), c0 = Cat(qx, qy);
+            float2 gr = G(qx + 1, qy), cr = Cat(qx + 1, qy);   /* R of the right quad */
+            float2 gd = G(qx, qy + 1), cd = Cat(qx, qy + 1);   /* R of the quad below */
+            float2 gl = G(qx - 1, qy), cl = Cat(qx - 1, qy);   /* B of the left quad */
+            float2 gu = G(qx, qy - 1), cu = Cat(qx, qy - 1);   /* B of the quad above */
+            float2 top = V2(x, y), bot = V2(x, y + 1);         /* R, Gr / Gb, B */
+            float o[4][3];
+            /* R */
+            o[0][0] = top.x; o[0][1] = g0.x; o[0][2] = c0.x;
+            /* B */
+            o[3][0] = c0.y; o[3][1] = g0.y; o[3][2] = bot.y;
+            {   /* Gr at (x + 1, y) */
+                float g00 = top.y, wt = W(x + 1, y).x;
+                float dh = 0.5f * ((top.x - g0.x) + (V(x + 2, y) - gr.x));
+                float ev = 0.5f * ((cu.y - gu.y) + (c0.y - g0.y));
+                float ch = wt * (g00 + ev) + (1.0f - wt) * (g00 + dh);
+                float dv = 0.5f * ((V(x + 1, y - 1) - gu.y) + (bot.y - g0.y));
+                float eh = 0.5f * ((c0.x - g0.x) + (cr.x - gr.x));
+                float cv = wt * (g00 + dv) + (1.0f - wt) * (g00 + eh);
+                o[1][0] = ch; o[1][1] = g00; o[1][2] = cv;
+            }
+            {   /* Gb at (x, y + 1) */
+                float g00 = bot.x, wt = W(x, y + 1).x;
+                float dh = 0.5f * ((V(x - 1, y + 1) - gl.y) + (bot.y - g0.y));
+                float ev = 0.5f * ((c0.x - g0.x) + (cd.x - gd.x));
+                float ch = wt * (g00 + ev) + (1.0f - wt) * (g00 + dh);
+                float dv = 0.5f * ((top.x - g0.x) + (V(x, y + 2) - gd.x));
+                float eh = 0.5f * ((cl.y - gl.y) + (c0.y - g0.y));
+                float cv = wt * (g00 + dv) + (1.0f - wt) * (g00 + eh);
+                o[2][0] = cv; o[2][1] = g00; o[2][2] = ch;
+            }
+            /* Pixels (x, y), (x + 1, y), (x, y + 1), (x + 1, y + 1) are quad
+             * sites 0, 1, 2, 3. */
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                *reinterpret_cast<float2 *>(&rgb[c * P + y * TW + x]) = make_float2(o[0][c], o[1][c]);
+                *reinterpret_cast<float2 *>(&rgb[c * P + (y + 1) * TW + x]) = make_float2(o[2][c], o[3][c]);
+            }
+        }
+        __syncthreads();
+    }
+};
+
+/* ------------------------------------------------------------- epilogue */
+
+/* From the tile's camera RGB (planar in shared memory, fp32, complete):
+ * the intermediate as it would be stored, then the colour stage into dst,
+ * or the chroma block means, and the AWB block records. */
+template <int TW, int TH, int NT>
+CRAW_DEV void epilogue(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, int y0, float *rgb)
+{
+    constexpr int P = TW * TH;
+    const bool chroma = io.quarter != nullptr;
+    for (int i = threadIdx.x; i < P; i += NT) {
+        int x = x0 + i % TW, y = y0 + i / TW;
+        float v[3] = { rgb[i], rgb[P + i], rgb[2 * P + i] };
+        if (k.fp16) {
+#pragma unroll
+            for (int c = 0; c < 3; c++) {
+                v[c] = craw_round_half(v[c]);
+                rgb[c * P + i] = v[c];
+            }
+        }
+        if (x >= k.width || y >= k.height)
+            continue;
+        if (io.inter)
+            craw_store_rgba(io.inter, io.inter_pitch, x, y, k.fp16, v[0], v[1], v[2]);
+        if (!chroma && io.dst) {
+            float o[3];
+            craw_color(k.color, v, o);
+            craw_store_rgba(io.dst, io.dst_pitch, x, y, io.dst_half, o[0], o[1], o[2]);
+        }
+    }
+    if (!chroma && !io.awb.rec)
+        return;
+    if (k.fp16)
+        __syncthreads();
+
+    if (chroma) {
+        /* 4x4 block means of (R - G, B - G, G), row by row over the pixels
+         * inside the frame (reference lib/ref/ref_chroma.c:49-74). */
+        const int qw = (k.width + 3) / 4, qh = (k.height + 3) / 4;
+        for (int b = threadIdx.x; b < (TW / 4) * (TH / 4); b += NT) {
+            int bx = b % (TW / 4), by = b / (TW / 4);
+            int qx = x0 / 4 + bx, qy = y0 / 4 + by;
+            if (qx >= qw || qy >= qh)
+                continue;
+            float s0 = 0.f, s1 = 0.f, s2 = 0.f, n = 0.f;
+            for (int jj = 0; jj < 4; jj++)
+                for (int ii = 0; ii < 4; ii++) {
+                    int x = bx * 4 + ii, y = by * 4 + jj;
+                    if (x0 + x >= k.width || y0 + y >= k.height)
+                        continue;
+                    int j = y * TW + x;
+                    float r = rgb[j], g = rgb[P + j], bl = rgb[2 * P + j];
+                    s0 = __fadd_rn(s0, __fsub_rn(r, g));
+                    s1 = __fadd_rn(s1, __fsub_rn(bl, g));
+                    s2 = __fadd_rn(s2, g);
+                    n += 1.0f;
+                }
+            craw_store_rgba(io.quarter, io.quarter_pitch, qx, qy, k.fp16,
+                            __fdiv_rn(s0, n), __fdiv_rn(s1, n), __fdiv_rn(s2, n));
+        }
+        return;
+    }
+
+    /* 8x8 block means, row by row (reference lib/awb.c:239-253). */
+    const int blocks_x = (k.width + 7) / 8;
+    for (int b = threadIdx.x; b < (TW / 8) * (TH / 8); b += NT) {
+        int bx = b % (TW / 8), by = b / (TW / 8);
+        if (x0 + bx * 8 >= k.width || y0 + by * 8 >= k.height)
+            continue;
+        int xe = min(8, k.width - (x0 + bx * 8)), ye = min(8, k.height - (y0 + by * 8));
+        float s0 = 0.f, s1 = 0.f, s2 = 0.f;
+        for (int jj = 0; jj < ye; jj++)
+            for (int ii = 0; ii < xe; ii++) {
+                int j = (by * 8 + jj) * TW + bx * 8 + ii;
+                s0 = __fadd_rn(s0, rgb[j]);
+                s1 = __fadd_rn(s1, rgb[P + j]);
+                s2 = __fadd_rn(s2, rgb[2 * P + j]);
+            }
+        float n = (float)(xe * ye);
+        io.awb.rec[(size_t)(y0 / 8 + by) * blocks_x + x0 / 8 + bx] =
+            craw_awb_block(__fdiv_rn(s0, n), __fdiv_rn(s1, n), __fdiv_rn(s2, n), k.awb_wb,
+                           io.awb.deferred, io.awb.nb_deferred);
+    }
+}
+
+/* ------------------------------------------------------------- kernels */
+
+template <int METHOD, int TW, int TH, int NT> struct PixelSmem {
     static constexpr int A = Apron<METHOD>::v;
     static constexpr int work = METHOD == kRcd ? RcdTile<TW, TH, NT>::floats
                                                : Tile<TW, TH, A, float>::N;
     static constexpr int floats = work + 3 * TW * TH;
 };
 
+/* Interior tiles of the RCD by quads (QTW x QTH pixels, all aprons inside
+ * the frame); the per-pixel kernel below takes the rest. */
+constexpr int QTW = 64, QTH = 16, QNT = 256, BTW = 32, BTH = 16;
+
+CRAW_DEV bool quad_interior(int x0, int y0, int w, int h)
+{
+    return x0 >= 6 && y0 >= 6 && x0 + QTW + 6 <= w && y0 + QTH + 6 <= h;
+}
+
+__global__ void __launch_bounds__(QNT)
+k_develop_rcd_quads(const CRAWKDevelop k, const CRAWKDevelopIO io)
+{
+    extern __shared__ __align__(16) float smem[];
+    const int x0 = blockIdx.x * QTW, y0 = blockIdx.y * QTH;
+    if (!quad_interior(x0, y0, k.width, k.height))
+        return;
+    RcdQuads<QTW, QTH, QNT> t;
+    t.carve(smem);
+    t.load(k, io, x0, y0);
+    __syncthreads();
+    t.run();
+    epilogue<QTW, QTH, QNT>(k, io, x0, y0, t.rgb);
+}
+
+/* Per-pixel tiles: every bilinear and MHC tile, and the RCD tiles that the
+ * quad kernel leaves (those whose QTW x QTH tile touches a border). */
 template <int METHOD, int TW, int TH, int NT>
 __global__ void __launch_bounds__(NT)
 k_develop(const CRAWKDevelop k, const CRAWKDevelopIO io)
@@ -280,8 +613,9 @@ k_develop(const CRAWKDevelop k, const CRAWKDevelopIO io)
     constexpr int A = Apron<METHOD>::v;
     constexpr int PPT = TW * TH / NT;
     static_assert(TW * TH % NT == 0 && TW % 8 == 0 && TH % 8 == 0, "tile shape");
-    __shared__ __align__(16) float smem[DevelopSmem<METHOD, TW, TH, NT>::floats];
-    float *rgb_s = smem + DevelopSmem<METHOD, TW, TH, NT>::work;
+    __shared__ __align__(16) float smem[PixelSmem<METHOD, TW, TH, NT>::floats];
+    float *rgb = smem + PixelSmem<METHOD, TW, TH, NT>::work;
+    constexpr int P = TW * TH;
 
     Frame f;
     f.x0 = blockIdx.x * TW;
@@ -290,8 +624,10 @@ k_develop(const CRAWKDevelop k, const CRAWKDevelopIO io)
     f.h = k.height;
     f.interior = f.x0 >= A && f.y0 >= A && f.x0 + TW + A <= k.width && f.y0 + TH + A <= k.height;
 
-    float out[PPT][3];
     if constexpr (METHOD == kRcd) {
+        static_assert(QTW % TW == 0 && QTH == TH, "a quad tile is whole per-pixel tiles");
+        if (quad_interior(f.x0 / QTW * QTW, f.y0, k.width, k.height))
+            return;
         RcdTile<TW, TH, NT> t;
         t.carve(smem);
         load_prepped<TW, TH, NT, 5>(k, io, f, t.v);
@@ -303,7 +639,11 @@ k_develop(const CRAWKDevelop k, const CRAWKDevelopIO io)
 #pragma unroll
         for (int j = 0; j < PPT; j++) {
             int i = threadIdx.x + j * NT, x = i % TW, y = i / TW;
-            t.pixel(x, y, ((f.y0 + y) & 1) * 2 + ((f.x0 + x) & 1), out[j]);
+            float o[3];
+            t.pixel(x, y, ((f.y0 + y) & 1) * 2 + ((f.x0 + x) & 1), o);
+            rgb[i] = o[0];
+            rgb[P + i] = o[1];
+            rgb[2 * P + i] = o[2];
         }
     } else {
         Tile<TW, TH, A, float> v;
@@ -314,90 +654,18 @@ k_develop(const CRAWKDevelop k, const CRAWKDevelopIO io)
         for (int j = 0; j < PPT; j++) {
             int i = threadIdx.x + j * NT, x = i % TW, y = i / TW;
             int s = ((f.y0 + y) & 1) * 2 + ((f.x0 + x) & 1);
-            if constexpr (METHOD == kBilinear)
-                bilinear_px(v, x, y, s, out[j]);
-            else
-                mhc_px(v, x, y, s, out[j]);
-        }
-    }
-
-    /* Epilogue: the intermediate as it would be stored, then whatever the
-     * frame needs of it. */
-    const bool chroma = io.quarter != nullptr;
-#pragma unroll
-    for (int j = 0; j < PPT; j++) {
-        int i = threadIdx.x + j * NT, x = f.x0 + i % TW, y = f.y0 + i / TW;
-        if (k.fp16) {
-#pragma unroll
-            for (int c = 0; c < 3; c++)
-                out[j][c] = craw_round_half(out[j][c]);
-        }
-        rgb_s[3 * i + 0] = out[j][0];
-        rgb_s[3 * i + 1] = out[j][1];
-        rgb_s[3 * i + 2] = out[j][2];
-        if (x >= k.width || y >= k.height)
-            continue;
-        if (io.inter)
-            craw_store_rgba(io.inter, io.inter_pitch, x, y, k.fp16, out[j][0], out[j][1], out[j][2]);
-        if (!chroma && io.dst) {
             float o[3];
-            craw_color(k.color, out[j], o);
-            craw_store_rgba(io.dst, io.dst_pitch, x, y, io.dst_half, o[0], o[1], o[2]);
+            if constexpr (METHOD == kBilinear)
+                bilinear_px(v, x, y, s, o);
+            else
+                mhc_px(v, x, y, s, o);
+            rgb[i] = o[0];
+            rgb[P + i] = o[1];
+            rgb[2 * P + i] = o[2];
         }
     }
-    if (!chroma && !io.awb.rec)
-        return;
     __syncthreads();
-
-    if (chroma) {
-        /* 4x4 block means of (R - G, B - G, G), summed row by row over the
-         * pixels inside the frame (reference lib/ref/ref_chroma.c:49-74). */
-        constexpr int QB = (TW / 4) * (TH / 4);
-        for (int b = threadIdx.x; b < QB; b += NT) {
-            int bx = b % (TW / 4), by = b / (TW / 4);
-            int qx = f.x0 / 4 + bx, qy = f.y0 / 4 + by;
-            int qw = (k.width + 3) / 4, qh = (k.height + 3) / 4;
-            if (qx >= qw || qy >= qh)
-                continue;
-            float s0 = 0.f, s1 = 0.f, s2 = 0.f, n = 0.f;
-            for (int jj = 0; jj < 4; jj++)
-                for (int ii = 0; ii < 4; ii++) {
-                    int x = bx * 4 + ii, y = by * 4 + jj;
-                    if (f.x0 + x >= k.width || f.y0 + y >= k.height)
-                        continue;
-                    const float *p = &rgb_s[3 * (y * TW + x)];
-                    s0 = __fadd_rn(s0, __fsub_rn(p[0], p[1]));
-                    s1 = __fadd_rn(s1, __fsub_rn(p[2], p[1]));
-                    s2 = __fadd_rn(s2, p[1]);
-                    n += 1.0f;
-                }
-            float m0 = __fdiv_rn(s0, n), m1 = __fdiv_rn(s1, n), m2 = __fdiv_rn(s2, n);
-            craw_store_rgba(io.quarter, io.quarter_pitch, qx, qy, k.fp16, m0, m1, m2);
-        }
-        return;
-    }
-
-    /* 8x8 block means, row by row (reference lib/awb.c:239-253). */
-    constexpr int AB = (TW / 8) * (TH / 8);
-    const int blocks_x = (k.width + 7) / 8;
-    for (int b = threadIdx.x; b < AB; b += NT) {
-        int bx = b % (TW / 8), by = b / (TW / 8);
-        if (f.x0 + bx * 8 >= k.width || f.y0 + by * 8 >= k.height)
-            continue;
-        int xe = min(8, k.width - (f.x0 + bx * 8)), ye = min(8, k.height - (f.y0 + by * 8));
-        float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-        for (int jj = 0; jj < ye; jj++)
-            for (int ii = 0; ii < xe; ii++) {
-                const float *p = &rgb_s[3 * ((by * 8 + jj) * TW + bx * 8 + ii)];
-                s0 = __fadd_rn(s0, p[0]);
-                s1 = __fadd_rn(s1, p[1]);
-                s2 = __fadd_rn(s2, p[2]);
-            }
-        float n = (float)(xe * ye);
-        uint64_t rec = craw_awb_block(__fdiv_rn(s0, n), __fdiv_rn(s1, n), __fdiv_rn(s2, n),
-                                      k.awb_wb, io.awb.deferred, io.awb.nb_deferred);
-        io.awb.rec[(size_t)(f.y0 / 8 + by) * blocks_x + f.x0 / 8 + bx] = rec;
-    }
+    epilogue<TW, TH, NT>(k, io, f.x0, f.y0, rgb);
 }
 
 template <int METHOD, int TW, int TH, int NT>
@@ -406,6 +674,23 @@ int launch(const CRAWKDevelop *k, const CRAWKDevelopIO *io, cudaStream_t s)
     dim3 grid((k->width + TW - 1) / TW, (k->height + TH - 1) / TH);
     k_develop<METHOD, TW, TH, NT><<<grid, NT, 0, s>>>(*k, *io);
     return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}
+
+int launch_rcd(const CRAWKDevelop *k, const CRAWKDevelopIO *io, cudaStream_t s)
+{
+    constexpr size_t smem = RcdQuads<QTW, QTH, QNT>::floats * sizeof(float);
+    static bool attr_set = false;
+    if (!attr_set) {
+        if (cudaFuncSetAttribute(k_develop_rcd_quads, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem) != cudaSuccess)
+            return -5;
+        attr_set = true;
+    }
+    dim3 grid((k->width + QTW - 1) / QTW, (k->height + QTH - 1) / QTH);
+    k_develop_rcd_quads<<<grid, QNT, smem, s>>>(*k, *io);
+    if (cudaGetLastError() != cudaSuccess)
+        return -5;
+    return launch<kRcd, BTW, BTH, 256>(k, io, s);
 }
 
 } // namespace
@@ -418,7 +703,7 @@ extern "C" int craw_k_develop(const CRAWKDevelop *k, const CRAWKDevelopIO *io, i
     switch (k->method) {
     case kBilinear: return launch<kBilinear, 64, 16, 256>(k, io, s);
     case kMhc:      return launch<kMhc, 64, 16, 256>(k, io, s);
-    case kRcd:      return launch<kRcd, 32, 16, 256>(k, io, s);
+    case kRcd:      return launch_rcd(k, io, s);
     default:        return -22;
     }
 }

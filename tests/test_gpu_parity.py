@@ -257,3 +257,19 @@ def test_edge_sizes(ctx, wh):
         got = run(ctx, m, pp, fp)
         ok, st = denoised_chain_ok(got, orc.process(m, pp, fp, "f32"))
         assert ok, (wh, st)
+
+
+@pytest.mark.parametrize("wh", [(640, 352), (518, 262)])
+def test_rcd_quad_tiles_vs_oracle(ctx, wh):
+    """Frames where most RCD tiles are interior (the quad kernel) and the
+    rest, including ragged last tiles, go through the per-pixel kernel."""
+    w, h = wh
+    m = frame(w, h, 81)
+    prof = W.make_profile()
+    pp = L.pipeline_params(w, h, debayer=L.DEBAYER_RCD, out_space=L.CS_XYZ_D65,
+                           out_format=L.FORMAT_RGBA32F, flags=L.FLAG_AWB_HISTOGRAM)
+    fp = L.frame_params(prof)
+    got = run(ctx, m, pp, fp)
+    ref = orc.process(m, pp, fp, "f32")
+    assert max_rel(got, ref) < TOL_FP32[L.DEBAYER_RCD], max_rel(got, ref)
+    assert max_rel(got, orc.process(m, pp, fp, "f64")) < 1e-3
