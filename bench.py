@@ -299,6 +299,7 @@ def run_gpu(args):
         return ms, stage, wall
 
     pipe = make_pipe(impl, storage)
+    kcfg = pipe.kernel_config()
     with ClockSampler(dev) as clk:
         ms, stage, wall = timed(pipe, args.steps, max(3, args.warmup))
     total_s = sum(ms) / 1000.0
@@ -388,7 +389,8 @@ def run_gpu(args):
                     "Poisson-Gaussian noise a=4 DN, b=40 DN^2), 4 frames in rotation",
             "config": {"workload": WORKLOAD, "width": w, "height": h, "impl": args.impl,
                        "storage": args.storage, "l2": "flushed between steps (256 MB write)",
-                       "parallelism": f"replicas x{ws}"},
+                       "parallelism": f"replicas x{ws}",
+                       "denoise_tile": ["2x8", "2x4"][kcfg[0]] + " (autotuned)"},
             "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
                            "max": lat[-1]},
             "stage_ms": {k: statistics.mean(v) for k, v in stage.items()},

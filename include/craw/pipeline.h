@@ -58,6 +58,13 @@ enum CRAWDebayer {
  * Without it the fused kernels never write the intermediate at all. */
 #define CRAW_PIPELINE_FLAG_KEEP_INTERMEDIATE        (1 << 16)
 
+/* Extension, no counterpart in the reference: skip the autotuner. By
+ * default craw_pipeline_create() of a denoising pipeline times every tile
+ * shape of the denoise kernel on a scratch frame of the pipeline's size and
+ * keeps the fastest (cached per size for the process); with this flag the
+ * default shape is used. */
+#define CRAW_PIPELINE_FLAG_NO_AUTOTUNE              (1 << 17)
+
 #define CRAW_FALSE_COLOR_MAX_PASSES 5
 #define CRAW_SHARPEN_MAX_RADIUS     2.0f
 #define CRAW_SHARPEN_MAX_ITERATIONS 100
@@ -233,5 +240,11 @@ CRAW_API int craw_pipeline_get_intermediate(CRAWPipeline *pipe, CRAWImage *rgb,
  * when no state is valid. */
 CRAW_API int craw_pipeline_get_temporal_state(CRAWPipeline *pipe, CRAWImage *level,
                                               CRAWImage *sqrt_var);
+
+/* Extension, no counterpart in the reference: the tile shapes the
+ * autotuner chose for the denoise kernel, without and with a temporal
+ * history (0: 2 columns x 8 rows a thread, 1: 2 x 4). */
+CRAW_API int craw_pipeline_get_kernel_config(CRAWPipeline *pipe, int *denoise_shape,
+                                             int *denoise_shape_history);
 
 #endif /* CRAW_PIPELINE_H */

@@ -54,6 +54,7 @@ FLAG_TEMPORAL_DENOISE = 1 << 7
 FLAG_SHARPEN = 1 << 8
 FLAG_PROFILE = 1 << 9
 FLAG_KEEP_INTERMEDIATE = 1 << 16
+FLAG_NO_AUTOTUNE = 1 << 17
 
 FRAME_CLAMP_NEGATIVE = 1 << 0
 FRAME_NO_GAMUT_COMPRESSION = 1 << 2
@@ -190,7 +191,7 @@ EXPORTS = (
     "craw_pipeline_free", "craw_pipeline_record", "craw_pipeline_get_awb_histogram",
     "craw_pipeline_get_awb_histogram_n", "craw_pipeline_get_stage_times",
     "craw_pipeline_get_stage_times_n", "craw_pipeline_get_intermediate",
-    "craw_pipeline_get_temporal_state",
+    "craw_pipeline_get_temporal_state", "craw_pipeline_get_kernel_config",
     "craw_profile_init", "craw_profile_validate", "craw_profile_eval",
     "craw_profile_noise_eval", "craw_noise_model_eval", "craw_colorspace_from_xyz_d65",
     "craw_colorspace_to_xyz_d65", "craw_planckian_xy", "craw_bradford_adaptation",
@@ -243,6 +244,7 @@ def lib() -> C.CDLL:
         "craw_pipeline_get_stage_times_n": (i32, [vp, u32, C.POINTER(StageTime), u32]),
         "craw_pipeline_get_intermediate": (i32, [vp, C.POINTER(Image), C.POINTER(Image)]),
         "craw_pipeline_get_temporal_state": (i32, [vp, C.POINTER(Image), C.POINTER(Image)]),
+        "craw_pipeline_get_kernel_config": (i32, [vp, C.POINTER(i32), C.POINTER(i32)]),
         "craw_profile_init": (None, [C.POINTER(Profile)]),
         "craw_profile_validate": (i32, [C.POINTER(Profile)]),
         "craw_profile_eval": (i32, [C.POINTER(Profile), i32, C.POINTER(Illuminant), C.POINTER(ColorParams)]),
@@ -447,6 +449,13 @@ class Pipeline:
         _check(lib().craw_pipeline_get_intermediate(self._h, C.byref(rgb), C.byref(mosaic)),
                "craw_pipeline_get_intermediate")
         return rgb, mosaic
+
+    def kernel_config(self) -> tuple[int, int]:
+        """The denoise tile shapes the autotuner chose (no history, history)."""
+        a, b = C.c_int(), C.c_int()
+        _check(lib().craw_pipeline_get_kernel_config(self._h, C.byref(a), C.byref(b)),
+               "craw_pipeline_get_kernel_config")
+        return a.value, b.value
 
     def temporal_state(self) -> tuple[Image, Image]:
         lvl, var = Image(), Image()

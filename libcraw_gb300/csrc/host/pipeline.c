@@ -20,6 +20,7 @@
  * stream, which is synchronised once at the end of creation).
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -70,7 +71,7 @@ struct CRAWPipeline {
     CRAWContext *ctx;
     CRAWPipelineParams params;
     bool has_denoise, has_temporal, has_chroma, awb, profile, keep, plain, fp16;
-    int dn_shape, dev_shape;
+    int dn_shape[2], dev_shape;   /* denoise tile shape without / with a history */
 
     /* Device memory. */
     uint16_t *clean;  size_t clean_pitch;
@@ -149,6 +150,141 @@ static void release(CRAWPipeline *p)
     free(p);
 }
 
+/* The autotuner: the fastest denoise tile shape for this frame size, with
+ * and without a temporal history, timed on the context's own stream over a
+ * scratch mosaic (the filter's work does not depend on the data), and
+ * remembered for the process so that a second pipeline of the same size
+ * starts at once. */
+#define TUNE_CACHE 32
+static struct tune_entry {
+    uint32_t w, h;
+    int shape[2];
+} tune_cache[TUNE_CACHE];
+static int tune_nb;
+static pthread_mutex_t tune_lock = PTHREAD_MUTEX_INITIALIZER;
+
+static int time_denoise(CRAWPipeline *p, const CRAWKDenoise *k, const CRAWKDenoiseIO *io, int shape,
+                        float *ms)
+{
+    CRAWContext *ctx = p->ctx;
+    cudaEvent_t e0, e1;
+    int ret = 0;
+    if (cudaEventCreate(&e0) != cudaSuccess)
+        return CRAW_ERROR(ENOMEM);
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return CRAW_ERROR(ENOMEM);
+    }
+    /* One launch to warm up, then the best of three. */
+    *ms = 1e30f;
+    for (int r = 0; r < 4 && ret == 0; r++) {
+        float t = 0.0f;
+        cudaEventRecord(e0, ctx->stream);
+        ret = craw_k_denoise(k, io, shape, ctx->stream);
+        cudaEventRecord(e1, ctx->stream);
+        if (ret == 0 && cudaEventSynchronize(e1) == cudaSuccess &&
+            cudaEventElapsedTime(&t, e0, e1) == cudaSuccess && r > 0 && t < *ms)
+            *ms = t;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ret < 0 ? CRAW_ERROR(EIO) : 0;
+}
+
+static int autotune(CRAWPipeline *p)
+{
+    CRAWContext *ctx = p->ctx;
+    const uint32_t w = p->params.width, h = p->params.height;
+    uint16_t *mosaic = NULL;
+    float *lvl = NULL;
+    uint8_t *var = NULL;
+    size_t mp, lp, vp;
+    int ret = 0;
+
+    pthread_mutex_lock(&tune_lock);
+    for (int i = 0; i < tune_nb; i++) {
+        if (tune_cache[i].w == w && tune_cache[i].h == h) {
+            p->dn_shape[0] = tune_cache[i].shape[0];
+            p->dn_shape[1] = tune_cache[i].shape[1];
+            pthread_mutex_unlock(&tune_lock);
+            return 0;
+        }
+    }
+    pthread_mutex_unlock(&tune_lock);
+
+    if ((ret = alloc_pitched(p, (void **)&mosaic, &mp, (size_t)w * 2, h)) < 0 ||
+        (ret = alloc_pitched(p, (void **)&lvl, &lp, (size_t)w * 4, h)) < 0 ||
+        (ret = alloc_pitched(p, (void **)&var, &vp, (size_t)w, h)) < 0)
+        goto done;
+    /* A mid-grey mosaic, a state of level 0.25 and unit variance. */
+    cudaMemset2DAsync(mosaic, mp, 0x08, (size_t)w * 2, h, ctx->stream);
+    cudaMemset2DAsync(lvl, lp, 0, (size_t)w * 4, h, ctx->stream);
+    cudaMemset2DAsync(var, vp, 0xff, (size_t)w, h, ctx->stream);
+    for (int hist = 0; hist < 2; hist++) {
+        CRAWKDenoise k;
+        CRAWKDenoiseIO io = {
+            .src = mosaic, .src_pitch = mp, .dst = p->clean, .dst_pitch = p->clean_pitch,
+            .lvl_prev = hist ? lvl : NULL, .lvl_next = hist ? lvl : NULL, .lvl_pitch = lp,
+            .var_prev = hist ? var : NULL, .var_next = hist ? var : NULL, .var_pitch = vp,
+        };
+        float best = 1e30f;
+        memset(&k, 0, sizeof(k));
+        k.pw = (int32_t)(w / 2);
+        k.ph = (int32_t)(h / 2);
+        k.gat_a = 1e-3f; k.gat_c = 1e-6f; k.gat_sc = 1e-3f; k.gat_fwd = 2000.0f;
+        k.gat_inv = 2.5e-4f; k.gat_off = 1e-3f; k.gat_t0 = 2.0f;
+        k.inv_h2 = 1.0f; k.t_alpha = 0.8f; k.t_inv_h2 = 1.0f;
+        k.guard_lo = 0.9f; k.guard_inv = 10.0f;
+        for (int s4 = 0; s4 < 4; s4++) {
+            k.black[s4] = 0.0f; k.inv_range[s4] = 16.0f; k.range[s4] = 0.0625f;
+        }
+        k.mode = CRAW_K_DN_SPATIAL | (hist ? CRAW_K_DN_TEMPORAL | CRAW_K_DN_HISTORY : 0);
+        if (!hist && !p->has_denoise)
+            continue;
+        if (hist && !p->has_temporal)
+            continue;
+        for (int shape = 0; shape < CRAW_K_DN_SHAPE_NB; shape++) {
+            float ms;
+            if ((ret = time_denoise(p, &k, &io, shape, &ms)) < 0)
+                goto done;
+            if (ms < best) {
+                best = ms;
+                p->dn_shape[hist] = shape;
+            }
+        }
+        craw_log(ctx, CRAW_LOG_VERBOSE, "autotune %ux%u %s: denoise shape %d, %.3f ms\n", w, h,
+                 hist ? "temporal" : "spatial", p->dn_shape[hist], (double)best);
+    }
+    pthread_mutex_lock(&tune_lock);
+    if (tune_nb < TUNE_CACHE && p->has_denoise && p->has_temporal) {
+        tune_cache[tune_nb].w = w;
+        tune_cache[tune_nb].h = h;
+        tune_cache[tune_nb].shape[0] = p->dn_shape[0];
+        tune_cache[tune_nb].shape[1] = p->dn_shape[1];
+        tune_nb++;
+    }
+    pthread_mutex_unlock(&tune_lock);
+done:
+    craw_dev_free(ctx, mosaic);
+    craw_dev_free(ctx, lvl);
+    craw_dev_free(ctx, var);
+    if (craw_dev_sync(ctx) < 0 && ret == 0)
+        ret = CRAW_ERROR(EIO);
+    return ret;
+}
+
+CRAW_API int craw_pipeline_get_kernel_config(CRAWPipeline *p, int *denoise_shape,
+                                             int *denoise_shape_history)
+{
+    if (!p)
+        return CRAW_ERROR(EINVAL);
+    if (denoise_shape)
+        *denoise_shape = p->dn_shape[0];
+    if (denoise_shape_history)
+        *denoise_shape_history = p->dn_shape[1];
+    return 0;
+}
+
 CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *params,
                                   CRAWPipeline **out)
 {
@@ -208,7 +344,7 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
     p->nb_slots = params->nb_awb_slots ? params->nb_awb_slots : 1;
     p->qw = (int)((w + 3) / 4);
     p->qh = (int)((h + 3) / 4);
-    p->dn_shape = CRAW_K_DN_SHAPE_2x8;
+    p->dn_shape[0] = p->dn_shape[1] = CRAW_K_DN_SHAPE_2x8;
 
     if ((p->has_denoise || p->has_temporal)) {
         /* The plane mirror holds for one reflection of the search + patch
@@ -294,6 +430,9 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
                     }
     }
     if ((ret = craw_dev_sync(ctx)) < 0)
+        goto fail;
+    if ((p->has_denoise || p->has_temporal) && !p->plain &&
+        !(params->flags & CRAW_PIPELINE_FLAG_NO_AUTOTUNE) && (ret = autotune(p)) < 0)
         goto fail;
     craw_log(ctx, CRAW_LOG_VERBOSE, "pipeline %ux%u debayer %d flags 0x%x storage %s impl %s\n",
              w, h, params->debayer, params->flags, p->fp16 ? "fp16" : "fp32",
@@ -575,7 +714,7 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
         }
         prof_begin(&pc, ST_DENOISE);
         ret = p->plain ? craw_k_plain_denoise(&dnk, &io, p->p_t, p->p_var, s)
-                       : craw_k_denoise(&dnk, &io, p->dn_shape, s);
+                       : craw_k_denoise(&dnk, &io, p->dn_shape[(dn_mode & CRAW_K_DN_HISTORY) != 0], s);
         prof_end(&pc);
         if (ret < 0)
             goto launch_fail;

@@ -281,15 +281,19 @@ struct RcdTile {
  *   Wp float2  pixels [-2, TW+2) x [-2, TH+2)   (wv, wp) weights
  *   Gq float2  quads  [-1, QW+1) x [-1, QH+1)   green at R and at B
  *   Cq float2  quads  [-1, QW+1) x [-1, QH+1)   B at R, R at B
- * Gq, Cq and the output planes reuse Dp's space once the weights exist. */
+ * Dp and Wp are stored as an even-column and an odd-column plane, so that
+ * the threads of a warp, one quad each, read consecutive elements of a
+ * plane rather than every other one. The output planes reuse Dp's space
+ * once the weights exist. */
 template <int TW, int TH, int NT>
 struct RcdQuads {
     static constexpr int QW = TW / 2, QH = TH / 2;
     static constexpr int VS = TW + 12, DS = TW + 8, WS = TW + 4, LS = QW + 4, GS = QW + 2;
     static constexpr int VN = (TH + 12) * VS, DN = (TH + 8) * DS, WN = (TH + 4) * WS;
     static constexpr int LN = (QH + 4) * LS, GN = (QH + 2) * GS;
-    static constexpr int floats = 4 * DN + 2 * WN + 2 * LN + VN;
-    static_assert(2 * GN * 2 + 3 * TW * TH <= 4 * DN, "G, C and the output fit in D's space");
+    static constexpr int DQ = DS / 2, WQ = WS / 2;           /* elements per plane row */
+    static constexpr int floats = 4 * DN + 2 * WN + 2 * LN + 4 * GN + VN;
+    static_assert(3 * TW * TH <= 4 * DN, "the output fits in D's space");
 
     float4 *Dp;
     float2 *Wp, *Lq, *Gq, *Cq;
@@ -301,10 +305,10 @@ struct RcdQuads {
         Dp = reinterpret_cast<float4 *>(base);
         Wp = reinterpret_cast<float2 *>(base + 4 * DN);
         Lq = reinterpret_cast<float2 *>(base + 4 * DN + 2 * WN);
-        Vp = base + 4 * DN + 2 * WN + 2 * LN;
-        Gq = reinterpret_cast<float2 *>(base);
-        Cq = reinterpret_cast<float2 *>(base + 2 * GN);
-        rgb = base + 4 * GN;
+        Gq = reinterpret_cast<float2 *>(base + 4 * DN + 2 * WN + 2 * LN);
+        Cq = reinterpret_cast<float2 *>(base + 4 * DN + 2 * WN + 2 * LN + 2 * GN);
+        Vp = base + 4 * DN + 2 * WN + 2 * LN + 4 * GN;
+        rgb = base;
     }
 
     CRAW_DEV float V(int x, int y) const { return Vp[(y + 6) * VS + x + 6]; }
@@ -312,8 +316,16 @@ struct RcdQuads {
     {
         return *reinterpret_cast<const float2 *>(&Vp[(y + 6) * VS + x + 6]);
     }
-    CRAW_DEV float4 &D(int x, int y) const { return Dp[(y + 4) * DS + x + 4]; }
-    CRAW_DEV float2 &W(int x, int y) const { return Wp[(y + 2) * WS + x + 2]; }
+    CRAW_DEV float4 &D(int x, int y) const
+    {
+        const int xx = x + 4;
+        return Dp[(xx & 1) * (DN / 2) + (y + 4) * DQ + (xx >> 1)];
+    }
+    CRAW_DEV float2 &W(int x, int y) const
+    {
+        const int xx = x + 2;
+        return Wp[(xx & 1) * (WN / 2) + (y + 2) * WQ + (xx >> 1)];
+    }
     CRAW_DEV float2 &Lat(int qx, int qy) const { return Lq[(qy + 2) * LS + qx + 2]; }
     CRAW_DEV float2 &G(int qx, int qy) const { return Gq[(qy + 1) * GS + qx + 1]; }
     CRAW_DEV float2 &Cat(int qx, int qy) const { return Cq[(qy + 1) * GS + qx + 1]; }
@@ -375,9 +387,12 @@ struct RcdQuads {
         }
         __syncthreads();
         /* Weights: 3x3 means of the discriminations, as three-wide row sums
-         * of a 4x4 window and then three of those rows. */
+         * of a 4x4 window and then three of those rows; and in the same
+         * pass, since it reads only its own quad's weights, green at R and
+         * at B. */
         for (int i = threadIdx.x; i < (QW + 2) * (QH + 2); i += NT) {
             const int qx = i % (QW + 2) - 1, qy = i / (QW + 2) - 1;
+            float wv[2][2];
             float4 h[4][2];
 #pragma unroll
             for (int r = 0; r < 4; r++) {
@@ -396,26 +411,19 @@ struct RcdQuads {
                     float4 o = b == 0 ? h[0][a] : h[3][a];
                     float vs = (o.x + mid.x) * (1.0f / 9.0f), hs = (o.y + mid.y) * (1.0f / 9.0f);
                     float ps = (o.z + mid.z) * (1.0f / 9.0f), qs = (o.w + mid.w) * (1.0f / 9.0f);
-                    W(2 * qx + a, 2 * qy + b) = make_float2(__fdividef(hs, hs + vs + RCD_EPS),
-                                                            __fdividef(qs, ps + qs + RCD_EPS));
+                    wv[b][a] = __fdividef(hs, hs + vs + RCD_EPS);
+                    W(2 * qx + a, 2 * qy + b) = make_float2(wv[b][a], __fdividef(qs, ps + qs + RCD_EPS));
                 }
             }
-        }
-        __syncthreads();
-        /* Green at R and at B (Gq lives where Dp was: D is dead now). */
-        for (int i = threadIdx.x; i < (QW + 2) * (QH + 2); i += NT) {
-            const int qx = i % (QW + 2) - 1, qy = i / (QW + 2) - 1;
             const int x = 2 * qx, y = 2 * qy;
             float2 l0 = Lat(qx, qy), lu = Lat(qx, qy - 1), ld = Lat(qx, qy + 1);
             float2 ll = Lat(qx - 1, qy), lr = Lat(qx + 1, qy);
             float gv = 0.5f * (V(x, y - 1) * (1.0f + rcd_ratio(l0.x, lu.x)) + V(x, y + 1) * (1.0f + rcd_ratio(l0.x, ld.x)));
             float gh = 0.5f * (V(x - 1, y) * (1.0f + rcd_ratio(l0.x, ll.x)) + V(x + 1, y) * (1.0f + rcd_ratio(l0.x, lr.x)));
-            float w0 = W(x, y).x;
-            float g_r = w0 * gv + (1.0f - w0) * gh;
+            float g_r = wv[0][0] * gv + (1.0f - wv[0][0]) * gh;
             gv = 0.5f * (V(x + 1, y) * (1.0f + rcd_ratio(l0.y, lu.y)) + V(x + 1, y + 2) * (1.0f + rcd_ratio(l0.y, ld.y)));
             gh = 0.5f * (V(x, y + 1) * (1.0f + rcd_ratio(l0.y, ll.y)) + V(x + 2, y + 1) * (1.0f + rcd_ratio(l0.y, lr.y)));
-            float w1 = W(x + 1, y + 1).x;
-            G(qx, qy) = make_float2(g_r, w1 * gv + (1.0f - w1) * gh);
+            G(qx, qy) = make_float2(g_r, wv[1][1] * gv + (1.0f - wv[1][1]) * gh);
         }
         __syncthreads();
         /* The missing colour at R (from the B diagonals) and at B (from the
