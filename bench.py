@@ -205,7 +205,7 @@ def run_reference(args):
     pp = L.pipeline_params(c.width, c.height, debayer=c.debayer, out_space=c.out_space, flags=c.flags,
                            out_format=L.FORMAT_RGBA32F)
     fp = L.frame_params(prof, **c.frame_kwargs())
-    frac = 0.125
+    frac = 0.5
     for _ in range(args.warmup):
         cpu_oracle_fps(frame, pp, fp, frac)
     times = []
@@ -377,7 +377,7 @@ def run_gpu(args):
     cpu = None
     if rank == 0 and not args.no_extras:
         cpu = cpu_oracle_fps(host_frames[0], L.pipeline_params(w, h, debayer=c.debayer, out_space=c.out_space,
-                                                              flags=c.flags), fp, 0.125)
+                                                              flags=c.flags), fp, 1.0)
 
     if rank == 0:
         clk_s = clk.summary()

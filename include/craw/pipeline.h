@@ -71,9 +71,10 @@ enum CRAWDebayer {
 #define CRAW_PIPELINE_PROFILE_SLOTS 4
 
 /* Storage of the intermediates (extension; zero is the default). FP32
- * keeps every intermediate in float. FP16 stores the camera RGB
- * intermediate and the chroma planes as half floats and keeps the VST
- * tiles in shared memory as half pairs; NLM weights, patch distances,
+ * keeps every intermediate in float. FP16 rounds the camera RGB
+ * intermediate to half floats (and stores it, and the chroma quarter
+ * planes, as half where they go to memory), as the reference's RGBA16F
+ * intermediate does; the VST planes, NLM weights and patch distances, the
  * colour matrices, the inverse VST, the temporal state and agreement test
  * and the histogram binning stay FP32. */
 enum CRAWStorage {
