@@ -373,6 +373,10 @@ def run_gpu(args):
         base = extras.get("plain_fp32", {}).get("fps")
         if base:
             extras["speedup_vs_plain_fp32"] = (args.steps / total_s) / base
+        extras["batch"] = run_batch_mix(ctx, stream, max(5, args.steps // 3), 3)
+        if base:
+            extras["batch"]["eq_speedup_vs_plain_fp32"] = (
+                extras["batch"]["fused_graph"]["eq_5760x3240_fps"] / base)
 
     cpu = None
     if rank == 0 and not args.no_extras:
@@ -413,6 +417,77 @@ def run_gpu(args):
     if ws > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def run_batch_mix(ctx, stream, steps: int, warmup: int) -> dict:
+    """The batched workload (16 frames of four sizes, NLM 1.0 + RCD + BT.2020
+    float32) as one recording of the batch API: a persistent fused launch
+    replayed from a captured CUDA graph; beside it the unfused and
+    graph-less variants and the same 16 frames through the single-frame
+    pipeline one after another. Inputs (336 MB) are larger than L2."""
+    import torch
+    import libcraw_gb300 as L
+    from libcraw_gb300 import workloads as W
+
+    mix = W.batch_mix()
+    prof = W.make_profile()
+    mw, mh = max(f.width for f in mix), max(f.height for f in mix)
+    srcs, dsts, fps, keep = [], [], [], []
+    for f in mix:
+        t = torch.from_numpy(f.frame().view(np.int16)).cuda()
+        o = torch.empty((f.height, f.width, 4), dtype=torch.float32, device="cuda")
+        keep += [t, o]
+        srcs.append(L.Image(t.data_ptr(), f.width * 2, L.FORMAT_R16_UNORM, f.width, f.height))
+        dsts.append(L.Image(o.data_ptr(), f.width * 16, L.FORMAT_RGBA32F, f.width, f.height))
+        fps.append(L.frame_params(prof, denoise_strength=1.0,
+                                  noise_override=W.noise_model(f.noise_a_dn, f.noise_b_dn)))
+    n_px = sum(f.width * f.height for f in mix)
+    sptr = stream.cuda_stream
+
+    def timed(record):
+        with torch.cuda.stream(stream):
+            for _ in range(warmup):
+                record()
+            torch.cuda.synchronize()
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(steps)]
+            for e0, e1 in evs:
+                e0.record(stream)
+                record()
+                e1.record(stream)
+            torch.cuda.synchronize()
+        ms = sorted(a.elapsed_time(b) for a, b in evs)
+        return {"ms_per_batch": statistics.mean(ms), "p50_ms": ms[len(ms) // 2], "max_ms": ms[-1],
+                "frames_per_s": len(mix) * 1000.0 / statistics.mean(ms),
+                "mpx_per_s": n_px / 1e3 / statistics.mean(ms),
+                "eq_5760x3240_fps": n_px / (5760 * 3240) * 1000.0 / statistics.mean(ms)}
+
+    res = {"workload": "16 frames: 6x1920x1080, 4x3840x2160, 4x5760x3240, 2x6000x4000; "
+                       "NLM 1.0 + RCD + BT.2020 float32; noise a~U[1,8], b~U[10,80] per frame",
+           "mpx": n_px / 1e6}
+    for name, flags in (("fused_graph", 0), ("unfused_graph", L.BATCH_FLAG_UNFUSED),
+                        ("fused_no_graph", L.BATCH_FLAG_NO_GRAPH)):
+        bp = L.batch_params(mw, mh, max_frames=len(mix), debayer=L.DEBAYER_RCD,
+                            out_space=L.CS_BT2020, flags=L.FLAG_DENOISE | flags)
+        with L.Batch(ctx, bp) as b:
+            res[name] = timed(lambda: b.record(sptr, srcs, dsts, fps))
+            res[name]["denoise_tile"] = ["2x4", "2x8"][b.info()["denoise_shape"]]
+    pipes = {}
+    for f in mix:
+        if (f.width, f.height) not in pipes:
+            pipes[(f.width, f.height)] = L.Pipeline(ctx, L.pipeline_params(
+                f.width, f.height, debayer=L.DEBAYER_RCD, out_space=L.CS_BT2020,
+                flags=L.FLAG_DENOISE, out_format=L.FORMAT_RGBA32F))
+
+    def singles():
+        for f, s_, d_, fp_ in zip(mix, srcs, dsts, fps):
+            pipes[(f.width, f.height)].record(sptr, s_, d_, fp_)
+    res["single_frame_pipeline"] = timed(singles)
+    for p_ in pipes.values():
+        p_.close()
+    res["speedup_vs_single_frames"] = (res["fused_graph"]["frames_per_s"] /
+                                       res["single_frame_pipeline"]["frames_per_s"])
+    return res
 
 
 def main():

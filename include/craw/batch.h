@@ -1,0 +1,65 @@
+/*
+ * craw-gb300: batched development (extension, no counterpart in the
+ * reference, which develops one frame per recording).
+ *
+ * A batch develops up to max_frames independent frames of different sizes
+ * in one persistent launch: every denoise tile of every frame, a
+ * grid-wide barrier, every develop tile of every frame. The launch is
+ * captured into a CUDA graph the first time a set of frame shapes is seen
+ * and replayed for every later recording with the same shapes; only the
+ * per-frame constants (a small table) are copied before each replay.
+ * Frames of a batch have no temporal history and no AWB histogram.
+ */
+#ifndef CRAW_BATCH_H
+#define CRAW_BATCH_H
+
+#include <craw/pipeline.h>
+
+typedef struct CRAWBatch CRAWBatch;
+
+/* Two persistent launches (denoise, then develop) instead of one launch
+ * with a grid-wide barrier. */
+#define CRAW_BATCH_FLAG_UNFUSED  (1u << 20)
+/* Launch directly on every recording instead of replaying a CUDA graph. */
+#define CRAW_BATCH_FLAG_NO_GRAPH (1u << 21)
+
+typedef struct CRAWBatchParams {
+    uint32_t max_frames;             /* frames one recording may carry, 1..64 */
+    uint32_t max_width, max_height;  /* the largest frame (even) */
+    enum CRAWDebayer debayer;        /* all frames of a batch */
+    enum CRAWColorSpace out_space;   /* default; a frame may override it */
+    CRAWFormat out_format;           /* CRAW_FORMAT_RGBA16F or CRAW_FORMAT_RGBA32F */
+    uint32_t flags;                  /* CRAW_PIPELINE_FLAG_DENOISE, CRAW_BATCH_FLAG_* */
+    uint8_t padding[64 - 7 * 4];
+} CRAWBatchParams;
+
+typedef struct CRAWBatchInfo {
+    int denoise_shape;               /* the autotuned tile shape: 0 = 2x4, 1 = 2x8 */
+    int fused;                       /* one launch with a grid barrier */
+    int graph;                       /* recordings replay a captured graph */
+    uint64_t captures, replays;      /* graphs captured, replays launched */
+} CRAWBatchInfo;
+
+CRAW_API void craw_batch_params_init(CRAWBatchParams *p);
+
+/* Allocates a denoised-mosaic buffer per frame slot, the constant table,
+ * and times the denoise tile shapes on a max_width x max_height scratch
+ * frame to pick the faster. */
+CRAW_API int craw_batch_create(CRAWContext *ctx, const CRAWBatchParams *params, CRAWBatch **out);
+
+/* Enqueues the development of `nb_frames` frames on `stream`: src[i]
+ * (R16_UNORM) -> dst[i] (out_format) with the settings fp[i] (the denoise
+ * strength and noise model, white balance, exposure, output space and
+ * their flags; temporal and chroma settings are ignored). Every frame is
+ * checked as craw_pipeline_record() checks it; a failed recording
+ * enqueues nothing. Recordings of one batch must be ordered (one stream,
+ * or events). */
+CRAW_API int craw_batch_record(CRAWBatch *b, cudaStream_t stream, uint32_t nb_frames,
+                               const CRAWImage *src, const CRAWImage *dst,
+                               const CRAWFrameParams *fp);
+
+CRAW_API int craw_batch_get_info(CRAWBatch *b, CRAWBatchInfo *info);
+
+CRAW_API void craw_batch_free(CRAWBatch **b);
+
+#endif /* CRAW_BATCH_H */

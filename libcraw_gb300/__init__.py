@@ -55,6 +55,8 @@ FLAG_SHARPEN = 1 << 8
 FLAG_PROFILE = 1 << 9
 FLAG_KEEP_INTERMEDIATE = 1 << 16
 FLAG_NO_AUTOTUNE = 1 << 17
+BATCH_FLAG_UNFUSED = 1 << 20
+BATCH_FLAG_NO_GRAPH = 1 << 21
 
 FRAME_CLAMP_NEGATIVE = 1 << 0
 FRAME_NO_GAMUT_COMPRESSION = 1 << 2
@@ -177,8 +179,19 @@ class StageTime(C.Structure):
     _fields_ = [("name", C.c_char_p), ("count", C.c_uint32), ("ms", C.c_double)]
 
 
+class BatchParams(C.Structure):
+    _fields_ = [("max_frames", C.c_uint32), ("max_width", C.c_uint32), ("max_height", C.c_uint32),
+                ("debayer", C.c_int), ("out_space", C.c_int), ("out_format", C.c_int),
+                ("flags", C.c_uint32), ("padding", C.c_uint8 * 36)]
+
+
+class BatchInfo(C.Structure):
+    _fields_ = [("denoise_shape", C.c_int), ("fused", C.c_int), ("graph", C.c_int),
+                ("captures", C.c_uint64), ("replays", C.c_uint64)]
+
+
 for _s, _n in ((Profile, 1264), (FrameParams, 264), (PipelineParams, 256), (CudaInitParams, 64),
-               (ContextOptions, 1024), (LensCorrection, 64)):
+               (ContextOptions, 1024), (LensCorrection, 64), (BatchParams, 64)):
     assert C.sizeof(_s) == _n, (_s.__name__, C.sizeof(_s), _n)
 
 # ----------------------------------------------------------------- library
@@ -196,6 +209,8 @@ EXPORTS = (
     "craw_profile_noise_eval", "craw_noise_model_eval", "craw_colorspace_from_xyz_d65",
     "craw_colorspace_to_xyz_d65", "craw_planckian_xy", "craw_bradford_adaptation",
     "craw_awb_histogram_from_rgb",
+    "craw_batch_params_init", "craw_batch_create", "craw_batch_record", "craw_batch_get_info",
+    "craw_batch_free",
 )
 
 
@@ -257,6 +272,11 @@ def lib() -> C.CDLL:
                                            C.POINTER(C.c_float * 9)]),
         "craw_awb_histogram_from_rgb": (i32, [vp, u32, u32, C.c_size_t, i32, C.POINTER(C.c_float * 3),
                                               vp, vp, vp]),
+        "craw_batch_params_init": (None, [C.POINTER(BatchParams)]),
+        "craw_batch_create": (i32, [vp, C.POINTER(BatchParams), C.POINTER(vp)]),
+        "craw_batch_record": (i32, [vp, vp, u32, C.POINTER(Image), C.POINTER(Image), C.POINTER(FrameParams)]),
+        "craw_batch_get_info": (i32, [vp, C.POINTER(BatchInfo)]),
+        "craw_batch_free": (None, [C.POINTER(vp)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -466,6 +486,56 @@ class Pipeline:
     def close(self) -> None:
         if self._h:
             lib().craw_pipeline_free(C.byref(self._h))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def batch_params(max_width: int, max_height: int, **kw) -> BatchParams:
+    p = BatchParams()
+    lib().craw_batch_params_init(C.byref(p))
+    p.max_width, p.max_height = max_width, max_height
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+class Batch:
+    """craw_batch_create / record / free: many frames of uneven sizes in
+    one persistent launch replayed from a CUDA graph."""
+
+    def __init__(self, ctx: Context, params: BatchParams):
+        self.ctx = ctx
+        self.params = params
+        self._h = C.c_void_p()
+        _check(lib().craw_batch_create(ctx.handle, C.byref(params), C.byref(self._h)),
+               "craw_batch_create")
+
+    def record(self, stream: int, src: list[Image], dst: list[Image], fp: list[FrameParams]) -> None:
+        n = len(src)
+        if len(dst) != n or len(fp) != n:
+            raise ValueError("src, dst and fp differ in length")
+        S, D, P = (Image * n)(*src), (Image * n)(*dst), (FrameParams * n)(*fp)
+        _check(lib().craw_batch_record(self._h, C.c_void_p(stream), n, S, D, P), "craw_batch_record")
+
+    def info(self) -> dict:
+        i = BatchInfo()
+        _check(lib().craw_batch_get_info(self._h, C.byref(i)), "craw_batch_get_info")
+        return {"denoise_shape": i.denoise_shape, "fused": bool(i.fused), "graph": bool(i.graph),
+                "captures": i.captures, "replays": i.replays}
+
+    def close(self) -> None:
+        if self._h:
+            lib().craw_batch_free(C.byref(self._h))
 
     def __enter__(self):
         return self

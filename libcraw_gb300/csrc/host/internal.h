@@ -37,6 +37,15 @@ int craw_dev_alloc(CRAWContext *ctx, void **ptr, size_t bytes);
 void craw_dev_free(CRAWContext *ctx, void *ptr);
 int craw_dev_sync(CRAWContext *ctx);
 
+/* Per-frame constants (frame.c). */
+int craw_image_check(CRAWContext *ctx, const CRAWImage *img, CRAWFormat fmt, uint32_t w, uint32_t h,
+                     const char *what);
+bool craw_images_overlap(const CRAWImage *a, const CRAWImage *b);
+int craw_develop_consts(CRAWContext *ctx, uint32_t w, uint32_t h, int debayer, bool fp16,
+                        enum CRAWColorSpace default_space, const CRAWFrameParams *fp, CRAWKDevelop *dk);
+int craw_denoise_consts(CRAWContext *ctx, uint32_t w, uint32_t h, const CRAWFrameParams *fp, int mode,
+                        CRAWKDenoise *k);
+
 /* Bins one deferred AWB block on the host, with the CPU builder's
  * arithmetic (lib/awb.c:270-291 of the reference). */
 void craw_awb_bin_host(float rr, float bb, float g, uint32_t *count, uint32_t *weight,

@@ -40,10 +40,6 @@ static_assert(sizeof(CRAWCudaInitParams) == 64, "CRAWCudaInitParams size");
 #define HIST_BYTES (3 * HIST_N * sizeof(uint32_t))
 #define DEFER_BYTES (CRAW_K_AWB_DEFER_MAX * sizeof(CRAWKAwbDeferred))
 
-/* Denoise constants, reference lib/pipeline.c:291-292. */
-#define DN_GUARD_LO 0.90f
-#define DN_GUARD_HI 1.00f
-
 #define MAX_STAGES 16
 
 enum { ST_DENOISE, ST_DEVELOP, ST_BLUR, ST_UP, ST_AWB, ST_NB };
@@ -453,92 +449,6 @@ CRAW_API void craw_pipeline_free(CRAWPipeline **pp)
     *pp = NULL;
 }
 
-static int image_check(CRAWPipeline *p, const CRAWImage *img, CRAWFormat fmt, const char *what)
-{
-    size_t bpp = fmt == CRAW_FORMAT_R16_UNORM ? 2 : (fmt == CRAW_FORMAT_RGBA16F ? 8 : 16);
-    if (img->format != fmt) {
-        craw_log(p->ctx, CRAW_LOG_ERROR, "%s format %d, expected %d\n", what, (int)img->format, (int)fmt);
-        return CRAW_ERROR(EINVAL);
-    }
-    if (img->width != p->params.width || img->height != p->params.height) {
-        craw_log(p->ctx, CRAW_LOG_ERROR, "%s is %ux%u, pipeline %ux%u\n", what, img->width,
-                 img->height, p->params.width, p->params.height);
-        return CRAW_ERROR(EINVAL);
-    }
-    if (!img->data || ((uintptr_t)img->data & 15) || (img->pitch & 15) ||
-        img->pitch < (size_t)img->width * bpp) {
-        craw_log(p->ctx, CRAW_LOG_ERROR, "%s needs 16-byte aligned data and pitch >= width * %zu\n",
-                 what, bpp);
-        return CRAW_ERROR(EINVAL);
-    }
-    return 0;
-}
-
-/* The frame's noise model: override when a > 0, else the profile's table
- * at as_shot_ei (reference lib/pipeline.c:1391-1409). */
-static int frame_noise_model(CRAWPipeline *p, const CRAWFrameParams *fp, CRAWNoiseModel *nm)
-{
-    int ret;
-    if (fp->noise_override.a > 0.0f) {
-        *nm = fp->noise_override;
-        return 0;
-    }
-    ret = craw_profile_noise_eval(fp->profile, fp->profile->as_shot_ei, nm);
-    if (ret < 0)
-        craw_log(p->ctx, CRAW_LOG_ERROR, "Denoising needs a noise model: the profile `%s` has no "
-                 "table and CRAWFrameParams.noise_override was not set\n",
-                 fp->profile->name[0] ? fp->profile->name : "(unnamed)");
-    return ret;
-}
-
-/* The denoise constants (reference lib/pipeline.c:1414-1467). */
-static int denoise_consts(CRAWPipeline *p, const CRAWFrameParams *fp, int mode, CRAWKDenoise *k)
-{
-    CRAWNoiseModel nm;
-    float a, b, c, h;
-    int ret = frame_noise_model(p, fp, &nm);
-    if (ret < 0)
-        return ret;
-    a = nm.a;
-    b = CRAW_MAX(nm.b, 0.0f);
-    if (!(a > 0.0f)) {
-        craw_log(p->ctx, CRAW_LOG_ERROR, "Noise model a = %g is not positive\n", (double)a);
-        return CRAW_ERROR(EINVAL);
-    }
-    c = 3.0f * a * a / 8.0f + b;
-    h = (mode & CRAW_K_DN_SPATIAL) ? fp->denoise_strength : 1.0f;
-    memset(k, 0, sizeof(*k));
-    k->pw = (int32_t)(p->params.width / 2);
-    k->ph = (int32_t)(p->params.height / 2);
-    k->gat_a = a;
-    k->gat_c = c;
-    k->gat_sc = sqrtf(c);
-    k->gat_fwd = 2.0f / a;
-    k->gat_inv = a / 4.0f;
-    k->gat_off = c / a;
-    k->gat_t0 = k->gat_fwd * k->gat_sc;
-    k->inv_h2 = 1.0f / (h * h);
-    k->t_alpha = (mode & CRAW_K_DN_TEMPORAL) ? fp->denoise_temporal_strength : 0.0f;
-    k->t_inv_h2 = 1.0f / (h * h);
-    k->guard_lo = DN_GUARD_LO;
-    k->guard_inv = 1.0f / (DN_GUARD_HI - DN_GUARD_LO);
-    k->mode = mode;
-    for (int s = 0; s < 4; s++) {
-        float range = fp->profile->white_level[s] - fp->profile->black_level[s];
-        k->black[s] = fp->profile->black_level[s];
-        k->inv_range[s] = 1.0f / range;
-        k->range[s] = range;
-    }
-    return 0;
-}
-
-static void mat3_mul_f(float out[3][3], const float a[3][3], const float b[3][3])
-{
-    for (int i = 0; i < 3; i++)
-        for (int j = 0; j < 3; j++)
-            out[i][j] = a[i][0] * b[0][j] + a[i][1] * b[1][j] + a[i][2] * b[2][j];
-}
-
 struct prof_ctx {
     CRAWPipeline *p;
     cudaStream_t s;
@@ -565,17 +475,13 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
                                   const CRAWImage *dst, const CRAWFrameParams *fp)
 {
     CRAWContext *ctx;
-    CRAWColorParams frame;
     CRAWKDevelop dk;
     CRAWKDevelopIO dio;
     CRAWKDenoise dnk;
     CRAWKChroma ck;
-    CRAWGamutCompress gc;
     struct prof_ctx pc = { 0 };
-    float m_out[3][3], scale;
     bool spatial, temporal, replay, denoise, chroma;
     int t_read, t_write, dn_mode = 0, ret;
-    enum CRAWColorSpace out_space;
     const uint16_t *mosaic;
     size_t mosaic_pitch;
     uint32_t w, h;
@@ -585,42 +491,16 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
     ctx = p->ctx;
     w = p->params.width;
     h = p->params.height;
-    if ((ret = image_check(p, src, CRAW_FORMAT_R16_UNORM, "Source")) < 0 ||
-        (ret = image_check(p, dst, p->params.out_format, "Destination")) < 0)
+    if ((ret = craw_image_check(ctx, src, CRAW_FORMAT_R16_UNORM, w, h, "Source")) < 0 ||
+        (ret = craw_image_check(ctx, dst, p->params.out_format, w, h, "Destination")) < 0)
         return ret;
-    {
-        uintptr_t s0 = (uintptr_t)src->data, s1 = s0 + src->pitch * h;
-        uintptr_t d0 = (uintptr_t)dst->data, d1 = d0 + dst->pitch * h;
-        if (s0 < d1 && d0 < s1) {
-            craw_log(ctx, CRAW_LOG_ERROR, "Source and destination must not alias\n");
-            return CRAW_ERROR(EINVAL);
-        }
+    if (craw_images_overlap(src, dst)) {
+        craw_log(ctx, CRAW_LOG_ERROR, "Source and destination must not alias\n");
+        return CRAW_ERROR(EINVAL);
     }
-
-    /* The prep applies the frame's own gains (reference pipeline.c:1773-1783). */
-    if ((ret = craw_profile_eval(fp->profile, fp->wb_mode, &fp->illuminant, &frame)) < 0)
+    if ((ret = craw_develop_consts(ctx, w, h, p->params.debayer, p->fp16, p->params.out_space, fp,
+                                   &dk)) < 0)
         return ret;
-    memset(&dk, 0, sizeof(dk));
-    dk.width = (int32_t)w;
-    dk.height = (int32_t)h;
-    dk.clip = 1.0f;
-    dk.method = p->params.debayer;
-    dk.fp16 = p->fp16;
-    for (int s4 = 0; s4 < 4; s4++) {
-        static const int chan[4] = { 0, 1, 1, 2 };
-        float range = fp->profile->white_level[s4] - fp->profile->black_level[s4];
-        if (!(range > 0.0f)) {
-            craw_log(ctx, CRAW_LOG_ERROR, "Profile site %d has white level %f <= black level %f\n",
-                     s4, fp->profile->white_level[s4], fp->profile->black_level[s4]);
-            return CRAW_ERROR(EINVAL);
-        }
-        dk.black[s4] = fp->profile->black_level[s4];
-        dk.range[s4] = range;
-        dk.inv_range[s4] = 1.0f / range;
-        dk.wbs[s4] = frame.wb[chan[s4]];
-    }
-    for (int c = 0; c < 3; c++)
-        dk.awb_wb[c] = frame.wb[c];
 
     /* Filters on or off for this frame, and the temporal sets (reference
      * pipeline.c:1785-1818): a replay reads what the last recording read
@@ -643,7 +523,7 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
     if (denoise) {
         dn_mode = (spatial ? CRAW_K_DN_SPATIAL : 0) | (temporal ? CRAW_K_DN_TEMPORAL : 0) |
                   (temporal && t_read >= 0 ? CRAW_K_DN_HISTORY : 0);
-        if ((ret = denoise_consts(p, fp, dn_mode, &dnk)) < 0)
+        if ((ret = craw_denoise_consts(ctx, w, h, fp, dn_mode, &dnk)) < 0)
             return ret;
     }
 
@@ -653,28 +533,6 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
                  (double)fp->denoise_chroma_strength);
         return CRAW_ERROR(EINVAL);
     }
-
-    /* Colour: M_out * cam_to_xyz * gain * 2^stops composed in float, RGC
-     * for ACEScg unless vetoed (reference pipeline.c:1899-1931). */
-    out_space = fp->out_space_set ? fp->out_space : p->params.out_space;
-    if ((ret = craw_colorspace_from_xyz_d65(out_space, m_out)) < 0) {
-        craw_log(ctx, CRAW_LOG_ERROR, "Unknown output colour space %d\n", (int)out_space);
-        return ret;
-    }
-    craw_gamut_compress_params(&gc);
-    mat3_mul_f(dk.color.m, m_out, frame.cam_to_xyz);
-    scale = frame.gain * exp2f(fp->exposure_stops);
-    for (int i = 0; i < 3; i++) {
-        for (int j = 0; j < 3; j++)
-            dk.color.m[i][j] *= scale;
-        dk.color.gc_thr[i] = gc.thr[i];
-        dk.color.gc_scl[i] = gc.scl[i];
-    }
-    dk.color.gc_pwr = gc.pwr;
-    dk.color.gc_inv_pwr = gc.inv_pwr;
-    dk.color.flags = (fp->flags & CRAW_FRAME_FLAG_CLAMP_NEGATIVE) ? CRAW_K_COLOR_CLAMP : 0;
-    if (out_space == CRAW_CS_ACES_AP1_LINEAR && !(fp->flags & CRAW_FRAME_FLAG_NO_GAMUT_COMPRESSION))
-        dk.color.flags |= CRAW_K_COLOR_RGC;
 
     /* Nothing can fail on the host from here on. */
     if (p->profile) {

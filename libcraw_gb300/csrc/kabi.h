@@ -139,6 +139,38 @@ int craw_k_chroma_up_color(const CRAWKDevelop *k, const CRAWKChroma *c,
  * caller), through shared-memory histograms with warp-aggregated atomics. */
 int craw_k_awb_reduce(const uint64_t *rec, uint32_t n, uint32_t *hist, cudaStream_t s);
 
+/* ------------------------------------------------------------- batch */
+
+/* One frame of a batch: its constants and buffers, how many tiles each
+ * phase has, and where its tiles start in each phase's item list. */
+typedef struct CRAWKBatchFrame {
+    CRAWKDenoise dn;            /* dn.mode == 0: the frame is not denoised */
+    CRAWKDenoiseIO dio;
+    CRAWKDevelop dv;
+    CRAWKDevelopIO vio;         /* vio.src is dio.dst when denoised */
+    int32_t dn_tx, dn_ty, dn_first;
+    int32_t dv_tx, dv_ty, dv_first;
+} CRAWKBatchFrame;
+
+/* Denoise tile shapes of the batch kernel (256 threads). */
+enum CRAWKBatchShape {
+    CRAW_K_BATCH_DN_2x4 = 0,    /* 2 columns x 4 rows a thread, 32x16 tiles */
+    CRAW_K_BATCH_DN_2x8,        /* 2 x 8, 32x32 tiles */
+    CRAW_K_BATCH_DN_NB,
+};
+
+/* Tiles per phase for a frame of w x h with a denoise shape. */
+void craw_k_batch_tiles(int32_t w, int32_t h, int shape, int32_t *dn_tx, int32_t *dn_ty,
+                        int32_t *dv_tx, int32_t *dv_ty);
+
+/* Develops the `nb` frames of the table `frames` (device memory) in one
+ * persistent launch: every denoise tile of every frame, a grid-wide
+ * barrier, every develop tile (`fused`); or as two persistent launches.
+ * Grid: as many CTAs as fit on the device at once. All frames use the
+ * same debayer, RCD or MHC or bilinear, `method`. */
+int craw_k_batch(const CRAWKBatchFrame *frames, int32_t nb, int32_t dn_items, int32_t dv_items,
+                 int method, int shape, int fused, cudaStream_t s);
+
 /* ------------------------------------------------------- plain baseline */
 
 /* One straightforward FP32 kernel per stage, each through device memory:

@@ -1,339 +1,22 @@
 /*
- * The raw-domain denoise: temporal recursive average + variance-
- * stabilising transform + non-local means on the four CFA planes, in one
- * launch (the reference's denoise_nlm pass; CPU definition
- * lib/ref/ref_denoise.c:168-336).
- *
- * One CTA filters the same OX x OY tile of all four planes, i.e. a
- * 2*OX x 2*OY region of the mosaic, so that the mosaic, the state and the
- * outputs move as whole 2x2 quads with 32-bit (mosaic) and 64-bit (state)
- * accesses. The stabilised planes of the tile and its search+patch apron
- * live in shared memory as FP32.
- *
- * The search: a thread owns BW columns x M rows of one plane. For a
- * search offset (dx, dy) it forms the squared differences of its own
- * (BW+2) x (M+2) window against the shifted one, sums them along x and
- * then along y in registers (sharing the middle pair of each three-sum),
- * and turns each of its BW*M patch distances into a weight with one ex2
- * on the MUFU. For one dy the shifted rows of all seven dx are a single
- * register block, read from shared memory once; dy is a runtime loop so
- * that the unrolled body of seven dx stays in the instruction cache.
+ * The raw-domain denoise kernel: one CTA per tile of the four CFA planes
+ * (the tile body is denoise_tile.cuh), and its launcher.
  */
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "common.cuh"
+#include "denoise_tile.cuh"
 
 namespace {
 
-constexpr int S = 3;     /* search radius, reference lib/pipeline.c:261 */
-constexpr int P = 1;     /* patch radius, reference lib/pipeline.c:262 */
-constexpr float kLog2e = 1.4426950408889634f;
-constexpr float kVarMin = 1.0e-4f;
-
-CRAW_DEV float gat_fwd(const CRAWKDenoise &k, float u)
-{
-    if (u >= 0.0f)
-        return k.gat_fwd * sqrtf(k.gat_a * u + k.gat_c);
-    return k.gat_t0 + __fdiv_rn(u, k.gat_sc);
-}
-
-CRAW_DEV float gat_inv(const CRAWKDenoise &k, float t)
-{
-    if (t >= k.gat_t0)
-        return k.gat_inv * t * t - k.gat_off;
-    return (t - k.gat_t0) * k.gat_sc;
-}
-
-CRAW_DEV float pick4(const float a[4], int i)
-{
-    return i == 0 ? a[0] : (i == 1 ? a[1] : (i == 2 ? a[2] : a[3]));
-}
-
-CRAW_DEV float level(const CRAWKDenoise &k, uint32_t raw, int pl)
-{
-    return ((float)raw * (1.0f / 65535.0f) - k.black[pl]) * k.inv_range[pl];
-}
-
-/* The four plane samples of mosaic quad (qx, qy): R, Gr, Gb, B. */
-CRAW_DEV void load_quad_u16(const CRAWKDenoiseIO &io, int qx, int qy, uint32_t q[4])
-{
-    const char *r0 = (const char *)io.src + (size_t)(2 * qy) * io.src_pitch;
-    uint32_t a = __ldg(reinterpret_cast<const uint32_t *>(r0) + qx);
-    uint32_t b = __ldg(reinterpret_cast<const uint32_t *>(r0 + io.src_pitch) + qx);
-    q[0] = a & 0xffffu; q[1] = a >> 16; q[2] = b & 0xffffu; q[3] = b >> 16;
-}
-
-CRAW_DEV void load_quad_f32(const float *base, size_t pitch, int qx, int qy, float q[4])
-{
-    const char *r0 = (const char *)base + (size_t)(2 * qy) * pitch;
-    float2 a = __ldg(reinterpret_cast<const float2 *>(r0) + qx);
-    float2 b = __ldg(reinterpret_cast<const float2 *>(r0 + pitch) + qx);
-    q[0] = a.x; q[1] = a.y; q[2] = b.x; q[3] = b.y;
-}
-
-template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY>
-struct Cfg {
-    static constexpr int R = SPATIAL ? S + P : 0;       /* apron of the tile */
-    static constexpr int OX = 16 * BW, OY = 2 * M * WP;  /* plane samples per tile */
-    static constexpr int TX = OX + 2 * R, TY = OY + 2 * R;
-    static constexpr int TS = (TX + 1) & ~1;             /* row stride, even for float2 */
-    static constexpr int TN = TY * TS;                   /* one plane's tile */
-    static constexpr int EX = TX + 2, EY = TY + 2;       /* history: one more ring */
-    static constexpr int EN = EX * EY;
-    static constexpr int NT = 4 * WP * 32;
-    static constexpr int smem_floats = 4 * TN * (HISTORY ? 2 : 1) + (HISTORY ? 8 * EN : 0);
-};
-
-/* The NLM search of one thread: BW columns x M rows of one plane, at the
- * tile position (ox0, oy0), over the 7x7 offsets (reference
- * lib/ref/ref_denoise.c:109-154). Weights as exp2 on the MUFU:
- * exp(-max(d2/(9h^2) - 2, 0)) = 2^min(d2 * c1 + c0, 0) with
- * c1 = -log2(e)/(9h^2), c0 = 2 log2(e); with a history
- * exp(-max(d2/(9h^2) - (vc + vq), 0) / vc) = 2^min((vc + vq - d2/(9h^2)) * log2(e)/vc, 0). */
-template <int BW, int M, int R, int TS, bool HISTORY>
-struct Search {
-    static_assert(BW % 2 == 0 && M % 2 == 0, "pairs of columns and rows");
-    float own[M + 2][BW + 2];
-    float acc[M][BW], wsum[M][BW];
-    float vc[HISTORY ? M : 1][BW], lvc[HISTORY ? M : 1][BW];
-    float kd, c1, c0;
-
-    CRAW_DEV void init(const float *Tp, const float *Vp, int ox0, int oy0, float inv_h2)
-    {
-#pragma unroll
-        for (int r = 0; r < M + 2; r++)
-#pragma unroll
-            for (int c = 0; c < BW + 2; c++)
-                own[r][c] = Tp[(oy0 + R - 1 + r) * TS + ox0 + R - 1 + c];
-        kd = (1.0f / 9.0f) * inv_h2;
-        c1 = -kLog2e * kd;
-        c0 = 2.0f * kLog2e;
-#pragma unroll
-        for (int m = 0; m < M; m++)
-#pragma unroll
-            for (int j = 0; j < BW; j++) {
-                acc[m][j] = 0.0f;
-                wsum[m][j] = 0.0f;
-                if constexpr (HISTORY) {
-                    vc[m][j] = Vp[(oy0 + R + m) * TS + ox0 + R + j];
-                    lvc[m][j] = __fdiv_rn(kLog2e, vc[m][j]);
-                }
-            }
-    }
-
-    /* All seven dx of one dy. The shifted rows of this dy, every column any
-     * dx reads, are one register block: rows oy0 + R - 1 + dy .. + M + 1,
-     * columns ox0 .. ox0 + BW + 2S + 1 (ox0 is even and R - 1 = S, so every
-     * float2 load is aligned), read once from shared memory for seven dx. */
-    CRAW_DEV void step_dy(const float *Tp, const float *Vp, int ox0, int oy0, int dy)
-    {
-        constexpr int WC = BW + 2 + 2 * S;
-        static_assert(R - 1 == S, "window origin");
-        float win[M + 2][WC];
-#pragma unroll
-        for (int r = 0; r < M + 2; r++) {
-            const float *row = Tp + (oy0 + R - 1 + dy + r) * TS + ox0;
-#pragma unroll
-            for (int c = 0; c < WC; c += 2) {
-                float2 t = *reinterpret_cast<const float2 *>(row + c);
-                win[r][c] = t.x;
-                win[r][c + 1] = t.y;
-            }
-        }
-        /* History: the variance of the shifted centres, columns
-         * ox0 + 1 .. ox0 + BW + 2S (loaded from ox0 in pairs). */
-        float vq[HISTORY ? M : 1][HISTORY ? BW + 2 * S + 2 : 1];
-        if constexpr (HISTORY) {
-#pragma unroll
-            for (int m = 0; m < M; m++) {
-                const float *row = Vp + (oy0 + R + dy + m) * TS + ox0;
-#pragma unroll
-                for (int c = 0; c < BW + 2 * S + 2; c += 2) {
-                    float2 t = *reinterpret_cast<const float2 *>(row + c);
-                    vq[m][c] = t.x;
-                    vq[m][c + 1] = t.y;
-                }
-            }
-        }
-#pragma unroll
-        for (int dx = -S; dx <= S; dx++) {
-            float hs[M + 2][BW];
-#pragma unroll
-            for (int r = 0; r < M + 2; r++) {
-                float e[BW + 2];
-#pragma unroll
-                for (int c = 0; c < BW + 2; c++) {
-                    float d = own[r][c] - win[r][c + dx + S];
-                    e[c] = d * d;
-                }
-                /* Row sums of three, the middle pair shared by two columns. */
-#pragma unroll
-                for (int j = 0; j < BW; j += 2) {
-                    float mid = e[j + 1] + e[j + 2];
-                    hs[r][j] = e[j] + mid;
-                    hs[r][j + 1] = mid + e[j + 3];
-                }
-            }
-#pragma unroll
-            for (int m = 0; m < M; m += 2) {
-#pragma unroll
-                for (int j = 0; j < BW; j++) {
-                    /* Column sums of three, the middle pair shared by two rows. */
-                    float mid = hs[m + 1][j] + hs[m + 2][j];
-                    float d2a = hs[m][j] + mid, d2b = mid + hs[m + 3][j];
-                    float wa, wb;
-                    if constexpr (HISTORY) {
-                        wa = craw_ex2(fminf(fmaf(d2a, -kd, vc[m][j] + vq[m][j + 1 + dx + S]) * lvc[m][j], 0.0f));
-                        wb = craw_ex2(fminf(fmaf(d2b, -kd, vc[m + 1][j] + vq[m + 1][j + 1 + dx + S]) * lvc[m + 1][j], 0.0f));
-                    } else {
-                        wa = craw_ex2(fminf(fmaf(d2a, c1, c0), 0.0f));
-                        wb = craw_ex2(fminf(fmaf(d2b, c1, c0), 0.0f));
-                    }
-                    wsum[m][j] += wa;
-                    wsum[m + 1][j] += wb;
-                    acc[m][j] = fmaf(wa, win[m + 1][j + 1 + dx + S], acc[m][j]);
-                    acc[m + 1][j] = fmaf(wb, win[m + 2][j + 1 + dx + S], acc[m + 1][j]);
-                }
-            }
-        }
-    }
-};
+using namespace craw_dn;
 
 template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY>
 __global__ void __launch_bounds__(Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>::NT)
 k_denoise(const CRAWKDenoise k, const CRAWKDenoiseIO io)
 {
-    using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>;
-    constexpr int R = C::R, OX = C::OX, OY = C::OY, TX = C::TX, TY = C::TY, TS = C::TS;
-    constexpr int NT = C::NT;
     extern __shared__ __align__(16) float smem[];
-    float *T = smem;                                 /* 4 planes of TN */
-    float *V = smem + 4 * C::TN;                     /* history: variance left */
-    float *TC = smem + 8 * C::TN;                    /* history: this frame, apron R+1 */
-    float *TPv = TC + 4 * C::EN;                     /* history: last frame, apron R+1 */
-
-    const int tx0 = blockIdx.x * OX, ty0 = blockIdx.y * OY;
-    const int tid = threadIdx.x;
-
-    /* ---- fill: the stabilised tile, temporally averaged when there is a
-     * history (reference lib/ref/ref_denoise.c:244-296). */
-    if constexpr (!HISTORY) {
-        for (int i = tid; i < TX * TY; i += NT) {
-            int r = i / TX, c = i % TX;
-            int qy = craw_mirror(ty0 - R + r, k.ph), qx = craw_mirror(tx0 - R + c, k.pw);
-            uint32_t q[4];
-            load_quad_u16(io, qx, qy, q);
-#pragma unroll
-            for (int pl = 0; pl < 4; pl++)
-                T[pl * C::TN + r * TS + c] = gat_fwd(k, level(k, q[pl], pl));
-        }
-    } else {
-        for (int i = tid; i < C::EN; i += NT) {
-            int r = i / C::EX, c = i % C::EX;
-            int qy = craw_mirror(ty0 - R - 1 + r, k.ph), qx = craw_mirror(tx0 - R - 1 + c, k.pw);
-            uint32_t q[4];
-            float lp[4];
-            load_quad_u16(io, qx, qy, q);
-            load_quad_f32(io.lvl_prev, io.lvl_pitch, qx, qy, lp);
-#pragma unroll
-            for (int pl = 0; pl < 4; pl++) {
-                TC[pl * C::EN + i] = gat_fwd(k, level(k, q[pl], pl));
-                TPv[pl * C::EN + i] = gat_fwd(k, lp[pl]);
-            }
-        }
-        __syncthreads();
-        for (int i = tid; i < TX * TY; i += NT) {
-            int r = i / TX, c = i % TX;
-            int qy = craw_mirror(ty0 - R + r, k.ph), qx = craw_mirror(tx0 - R + c, k.pw);
-            const char *vr = (const char *)io.var_prev + (size_t)(2 * qy) * io.var_pitch;
-            uint16_t v0 = __ldg(reinterpret_cast<const uint16_t *>(vr) + qx);
-            uint16_t v1 = __ldg(reinterpret_cast<const uint16_t *>(vr + io.var_pitch) + qx);
-            uint32_t sv[4] = { v0 & 0xffu, (uint32_t)v0 >> 8, v1 & 0xffu, (uint32_t)v1 >> 8 };
-#pragma unroll
-            for (int pl = 0; pl < 4; pl++) {
-                const float *cp = TC + pl * C::EN, *pp = TPv + pl * C::EN;
-                int e0 = (r + 1) * C::EX + c + 1;
-                float d2 = 0.0f;
-#pragma unroll
-                for (int ky = -1; ky <= 1; ky++)
-#pragma unroll
-                    for (int kx = -1; kx <= 1; kx++) {
-                        float e = pp[e0 + ky * C::EX + kx] - cp[e0 + ky * C::EX + kx];
-                        d2 = __fadd_rn(d2, __fmul_rn(e, e));
-                    }
-                float x = d2 * (1.0f / 9.0f) * k.t_inv_h2 - 2.0f;
-                float a = k.t_alpha * expf(-fmaxf(x, 0.0f));
-                float sp = (float)sv[pl] * (1.0f / 255.0f);
-                float vv = __fadd_rn(__fmul_rn(1.0f - a, 1.0f - a), __fmul_rn(a * a, sp * sp));
-                T[pl * C::TN + r * TS + c] = __fadd_rn(__fmul_rn(cp[e0], 1.0f - a), __fmul_rn(pp[e0], a));
-                V[pl * C::TN + r * TS + c] = fmaxf(vv, kVarMin);
-            }
-        }
-    }
-    __syncthreads();
-
-    /* ---- the search */
-    const int warp = tid >> 5, lane = tid & 31;
-    const int pl = warp / WP, band = warp % WP;
-    const int ox0 = (lane & 15) * BW, oy0 = ((band << 1) | (lane >> 4)) * M;
-    const float *Tp = T + pl * C::TN;
-    float res[M][BW];
-
-    if constexpr (SPATIAL) {
-        const float *Vp = V + pl * C::TN;
-        Search<BW, M, R, TS, HISTORY> st;
-        st.init(Tp, Vp, ox0, oy0, k.inv_h2);
-        /* dy is a runtime loop and only the seven dx of one dy are
-         * unrolled, so that the loop body stays in the instruction cache. */
-#pragma unroll 1
-        for (int dy = -S; dy <= S; dy++)
-            st.step_dy(Tp, Vp, ox0, oy0, dy);
-#pragma unroll
-        for (int m = 0; m < M; m++)
-#pragma unroll
-            for (int j = 0; j < BW; j++)
-                res[m][j] = __fdiv_rn(st.acc[m][j], st.wsum[m][j]);
-    }
-
-    /* ---- outputs: the next state, and the denoised mosaic in its raw
-     * encoding after the highlight guard (reference
-     * lib/ref/ref_denoise.c:285-324). */
-    const int px = pl & 1, py = pl >> 1;
-    /* This warp's plane constants, selected once (indexing the parameter
-     * arrays with the warp's plane would copy them to local memory). */
-    const float blk = pick4(k.black, pl), irng = pick4(k.inv_range, pl), rng = pick4(k.range, pl);
-#pragma unroll
-    for (int m = 0; m < M; m++) {
-        const int qy = ty0 + oy0 + m;
-#pragma unroll
-        for (int j = 0; j < BW; j++) {
-            const int qx = tx0 + ox0 + j;
-            if (qy >= k.ph || qx >= k.pw)
-                continue;
-            const int my = 2 * qy + py, mx = 2 * qx + px;
-            const float tc = Tp[(oy0 + R + m) * TS + ox0 + R + j];
-            if constexpr (TEMPORAL) {
-                float *lr = (float *)((char *)io.lvl_next + (size_t)my * io.lvl_pitch);
-                uint8_t *vr = io.var_next + (size_t)my * io.var_pitch;
-                lr[mx] = gat_inv(k, tc);
-                if constexpr (HISTORY) {
-                    float vv = V[pl * C::TN + (oy0 + R + m) * TS + ox0 + R + j];
-                    vr[mx] = (uint8_t)rintf(sqrtf(fminf(fmaxf(vv, 0.0f), 1.0f)) * 255.0f);
-                } else {
-                    vr[mx] = 255;
-                }
-            }
-            float u = gat_inv(k, SPATIAL ? res[m][j] : tc);
-            uint16_t raw0 = __ldg((const uint16_t *)((const char *)io.src + (size_t)my * io.src_pitch) + mx);
-            float u0 = ((float)raw0 * (1.0f / 65535.0f) - blk) * irng;
-            float gr = fminf(fmaxf((u0 - k.guard_lo) * k.guard_inv, 0.0f), 1.0f);
-            u = u + (u0 - u) * gr;
-            float ro = fminf(fmaxf(blk + u * rng, 0.0f), 1.0f);
-            uint16_t *dr = (uint16_t *)((char *)io.dst + (size_t)my * io.dst_pitch);
-            dr[mx] = (uint16_t)rintf(ro * 65535.0f);
-        }
-    }
+    denoise_tile<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>(k, io, blockIdx.x, blockIdx.y, smem);
 }
 
 template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY>

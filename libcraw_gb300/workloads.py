@@ -163,3 +163,32 @@ def config(n: int, width: int | None = None, height: int | None = None) -> Confi
     if height:
         c.height = height
     return c
+
+
+@dataclass
+class BatchFrame:
+    width: int
+    height: int
+    seed: int
+    noise_a_dn: float
+    noise_b_dn: float
+
+    def frame(self, out: np.ndarray | None = None) -> np.ndarray:
+        return synth_frame(self.width, self.height, self.seed, rects=256, zone_plates=4,
+                           noise_a_dn=self.noise_a_dn, noise_b_dn=self.noise_b_dn, out=out)
+
+
+def batch_mix(scale: int = 1) -> list[BatchFrame]:
+    """The batched workload: 6 x 1920x1080, 4 x 3840x2160, 4 x 5760x3240 and
+    2 x 6000x4000 frames, independent seeds, noise a ~ U[1, 8] DN and
+    b ~ U[10, 80] DN^2 per frame; ``scale`` divides every side (rounded to
+    even) for tests."""
+    rng = np.random.default_rng(4004)
+    sizes = [(1920, 1080)] * 6 + [(3840, 2160)] * 4 + [(5760, 3240)] * 4 + [(6000, 4000)] * 2
+    out = []
+    for i, (w, h) in enumerate(sizes):
+        a, b = float(rng.uniform(1.0, 8.0)), float(rng.uniform(10.0, 80.0))
+        out.append(BatchFrame(max(12, w // scale // 2 * 2), max(12, h // scale // 2 * 2),
+                              40040 + i, a, b))
+    return out
+
