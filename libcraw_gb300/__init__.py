@@ -63,6 +63,7 @@ FRAME_NO_GAMUT_COMPRESSION = 1 << 2
 FRAME_TEMPORAL_RESET = 1 << 4
 
 AWB_BINS = 128
+AWB_NOALLOC_MAX_BLOCKS = 1 << 18
 PROFILE_SLOTS = 4
 
 # ----------------------------------------------------------------- structs
@@ -210,7 +211,7 @@ EXPORTS = (
     "craw_colorspace_to_xyz_d65", "craw_planckian_xy", "craw_bradford_adaptation",
     "craw_awb_histogram_from_rgb",
     "craw_batch_params_init", "craw_batch_create", "craw_batch_record", "craw_batch_get_info",
-    "craw_batch_free",
+    "craw_batch_free", "craw_awb_histogram_from_rgb_cuda_noalloc",
 )
 
 
@@ -277,6 +278,8 @@ def lib() -> C.CDLL:
         "craw_batch_record": (i32, [vp, vp, u32, C.POINTER(Image), C.POINTER(Image), C.POINTER(FrameParams)]),
         "craw_batch_get_info": (i32, [vp, C.POINTER(BatchInfo)]),
         "craw_batch_free": (None, [C.POINTER(vp)]),
+        "craw_awb_histogram_from_rgb_cuda_noalloc": (i32, [vp, u32, u32, C.c_size_t, i32,
+                                                           C.POINTER(C.c_float * 3), vp, vp, vp, vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
