@@ -3,8 +3,9 @@
  * (reference include/craw/awb.h).
  *
  * The GPU reduces each frame to a 2D histogram of raw chromaticity with
- * three counters per bin; the host reads it back. The estimator that
- * searches it is not part of this library's path.
+ * three counters per bin; the host reads it back, estimates the frame's
+ * illuminant from it (craw_awb_estimate) and smooths the estimates of a
+ * stream into a track (craw_awb_smoother_*).
  */
 #ifndef CRAW_AWB_H
 #define CRAW_AWB_H
@@ -44,6 +45,96 @@ CRAW_API int craw_awb_histogram_from_rgb(const float *rgb, uint32_t width,
                                          int channels, const float wb_applied[3],
                                          uint32_t *count, uint32_t *weight,
                                          uint32_t *weight_bright);
+
+/* ----------------------------------------------------------- estimator */
+
+/* Parameters of craw_awb_estimate(), the reference's (awb.h:62-89). */
+typedef struct CRAWAwbParams {
+    float band;                     /* neutral band around the locus, ln-ratio units; 0.08 */
+    float sigma;                    /* Gaussian falloff of a bin's weight with its distance; 0.05 */
+    float min_zone_fraction;        /* share of the mass inside the band below which the
+                                     * reading is invalid; 0.02 */
+    float ambience;                 /* 0: correct fully; 1: keep the warmth below the knee */
+    float ambience_knee_cct;        /* 4000 */
+    float cct_min, cct_max;         /* clamps of the reported cct; 0: the table's range */
+    bool prefer_bright;             /* take the g^4 reading when it is valid; true */
+    float bright_max_spread_mired;  /* the g^4 reading's spread limit along the locus; 60 */
+} CRAWAwbParams;
+
+CRAW_API void craw_awb_params_init(CRAWAwbParams *p);
+
+/* One reading of the histogram under one weighting. */
+typedef struct CRAWAwbCandidate {
+    bool valid;
+    CRAWIlluminant illuminant;      /* before ambience and clamping */
+    float in_zone_fraction;         /* share of the weighting's mass inside the band */
+    float spread_mired;             /* weighted standard deviation along the locus */
+} CRAWAwbCandidate;
+
+enum CRAWAwbSource {
+    CRAW_AWB_SOURCE_NONE = 0,
+    CRAW_AWB_SOURCE_ZONE,           /* the min(g, 0.5) weighted neutral bins */
+    CRAW_AWB_SOURCE_BRIGHT,         /* the g^4 weighted ones */
+};
+
+typedef struct CRAWAwbEstimate {
+    bool valid;
+    CRAWIlluminant illuminant;      /* the chosen reading after ambience and clamping */
+    float confidence;               /* 0..1, from the in-band share and the spread */
+    float in_zone_fraction;
+    float spread_mired;
+    enum CRAWAwbSource source;
+    CRAWAwbCandidate zone, bright;
+} CRAWAwbEstimate;
+
+/* The illuminant of one frame from its histogram (a pipeline's
+ * craw_pipeline_get_awb_histogram()): every occupied bin centre is taken as
+ * a neutral, placed on the profile's locus, and weighted by its two
+ * counters and a Gaussian of its distance from the locus; the in-band
+ * weighted means give two readings, of which the bright one wins when it
+ * is valid and preferred. `params` NULL means the defaults. Needs a white
+ * balance table of two knots or more. Reference awb.h:115-123
+ * (lib/awb.c:86-211). */
+CRAW_API int craw_awb_estimate(const CRAWProfile *p, const CRAWAwbHistogram *hist,
+                               const CRAWAwbParams *params, CRAWAwbEstimate *out);
+
+/* ------------------------------------------------------------ smoother */
+
+/* A per-stream illuminant track kept in mired (reference awb.h:141-180,
+ * lib/awb_smoother.c): exponential smoothing with a time constant, a
+ * hysteresis dead band and a slew limit; estimates below min_confidence
+ * hold the track; a scene cut with a confident estimate restarts it. */
+typedef struct CRAWAwbSmoother CRAWAwbSmoother;
+
+typedef struct CRAWAwbSmootherParams {
+    float time_constant;            /* seconds; 1.0 */
+    float hysteresis_mired;         /* 3.0 */
+    float max_slew_mired_per_s;     /* 30.0 */
+    float min_confidence;           /* 0.2 */
+} CRAWAwbSmootherParams;
+
+CRAW_API void craw_awb_smoother_params_init(CRAWAwbSmootherParams *p);
+/* `params` NULL means the defaults; non-finite or non-positive time
+ * constant or slew, or a negative hysteresis, is CRAW_ERROR(EINVAL). */
+CRAW_API int craw_awb_smoother_create(const CRAWAwbSmootherParams *params,
+                                      CRAWAwbSmoother **sm);
+CRAW_API void craw_awb_smoother_free(CRAWAwbSmoother **sm);
+/* Forgets the track: the next push starts one. */
+CRAW_API void craw_awb_smoother_reset(CRAWAwbSmoother *sm);
+/* Puts the track at `illum` as of `pts_s` (a seed, e.g. the camera's own
+ * balance); an illuminant that is not finite and positive is ignored. */
+CRAW_API void craw_awb_smoother_set(CRAWAwbSmoother *sm, double pts_s,
+                                    const CRAWIlluminant *illum);
+/* Feeds the estimate of the frame at `pts_s` and returns the illuminant to
+ * apply to it. The first usable estimate starts the track whatever its
+ * confidence; with no track and no usable estimate the call returns
+ * CRAW_ERROR(EAGAIN) and leaves `out` as it was. The step is clamped to
+ * [0, 1] s of presentation time. */
+CRAW_API int craw_awb_smoother_push(CRAWAwbSmoother *sm, double pts_s,
+                                    const CRAWAwbEstimate *est, bool scene_cut,
+                                    CRAWIlluminant *out);
+
+/* ------------------------------------------------------------ no-alloc */
 
 /* The most 8x8 blocks craw_awb_histogram_from_rgb_cuda_noalloc() takes:
  * a 4096 x 4096 image, or any other whose ceil(w/8) * ceil(h/8) fits. */

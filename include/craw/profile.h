@@ -115,6 +115,27 @@ CRAW_API int craw_profile_eval(const CRAWProfile *p, enum CRAWWbMode mode,
                                const CRAWIlluminant *illum,
                                CRAWColorParams *out);
 
+/* The illuminant under which a neutral surface gives the raw ratios
+ * (raw_rg, raw_bg) = (R/G, B/G) before white balance: out->cct is the
+ * point of the white balance locus that the neutral lies from along the
+ * green direction (ln R/G and ln B/G moving together, the direction of a
+ * tint), out->tint the signed distance along it, so that
+ * craw_profile_illuminant_to_neutral() returns the ratios wherever the
+ * table reaches. A neutral beyond either end of the locus goes to that
+ * end. Needs a white balance table of two knots or more
+ * (CRAW_ERROR(ENOTSUP)); ratios that are not finite and positive are
+ * CRAW_ERROR(EINVAL). Reference profile.h:169-181 (lib/profile.c:254-389). */
+CRAW_API int craw_profile_neutral_to_illuminant(const CRAWProfile *p,
+                                                float raw_rg, float raw_bg,
+                                                CRAWIlluminant *out);
+
+/* The raw ratios of a neutral surface under `illum` (its cct clamped to
+ * the table): the inverse of the gains craw_profile_eval() applies with
+ * CRAW_WB_REBALANCE. Reference profile.h:183-187 (lib/profile.c:391-418). */
+CRAW_API int craw_profile_illuminant_to_neutral(const CRAWProfile *p,
+                                                const CRAWIlluminant *illum,
+                                                float *raw_rg, float *raw_bg);
+
 /* Output colour spaces, linear and scene referred. Values as the
  * reference's (profile.h:207-216). */
 enum CRAWColorSpace {

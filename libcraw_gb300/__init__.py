@@ -180,6 +180,29 @@ class StageTime(C.Structure):
     _fields_ = [("name", C.c_char_p), ("count", C.c_uint32), ("ms", C.c_double)]
 
 
+class AwbParams(C.Structure):
+    _fields_ = [("band", C.c_float), ("sigma", C.c_float), ("min_zone_fraction", C.c_float),
+                ("ambience", C.c_float), ("ambience_knee_cct", C.c_float), ("cct_min", C.c_float),
+                ("cct_max", C.c_float), ("prefer_bright", C.c_bool),
+                ("bright_max_spread_mired", C.c_float)]
+
+
+class AwbCandidate(C.Structure):
+    _fields_ = [("valid", C.c_bool), ("illuminant", Illuminant), ("in_zone_fraction", C.c_float),
+                ("spread_mired", C.c_float)]
+
+
+class AwbEstimate(C.Structure):
+    _fields_ = [("valid", C.c_bool), ("illuminant", Illuminant), ("confidence", C.c_float),
+                ("in_zone_fraction", C.c_float), ("spread_mired", C.c_float), ("source", C.c_int),
+                ("zone", AwbCandidate), ("bright", AwbCandidate)]
+
+
+class AwbSmootherParams(C.Structure):
+    _fields_ = [("time_constant", C.c_float), ("hysteresis_mired", C.c_float),
+                ("max_slew_mired_per_s", C.c_float), ("min_confidence", C.c_float)]
+
+
 class BatchParams(C.Structure):
     _fields_ = [("max_frames", C.c_uint32), ("max_width", C.c_uint32), ("max_height", C.c_uint32),
                 ("debayer", C.c_int), ("out_space", C.c_int), ("out_format", C.c_int),
@@ -192,7 +215,8 @@ class BatchInfo(C.Structure):
 
 
 for _s, _n in ((Profile, 1264), (FrameParams, 264), (PipelineParams, 256), (CudaInitParams, 64),
-               (ContextOptions, 1024), (LensCorrection, 64), (BatchParams, 64)):
+               (ContextOptions, 1024), (LensCorrection, 64), (BatchParams, 64), (AwbParams, 36),
+               (AwbCandidate, 20), (AwbEstimate, 68), (AwbSmootherParams, 16)):
     assert C.sizeof(_s) == _n, (_s.__name__, C.sizeof(_s), _n)
 
 # ----------------------------------------------------------------- library
@@ -212,6 +236,10 @@ EXPORTS = (
     "craw_awb_histogram_from_rgb",
     "craw_batch_params_init", "craw_batch_create", "craw_batch_record", "craw_batch_get_info",
     "craw_batch_free", "craw_awb_histogram_from_rgb_cuda_noalloc",
+    "craw_profile_neutral_to_illuminant", "craw_profile_illuminant_to_neutral",
+    "craw_awb_params_init", "craw_awb_estimate", "craw_awb_smoother_params_init",
+    "craw_awb_smoother_create", "craw_awb_smoother_free", "craw_awb_smoother_reset",
+    "craw_awb_smoother_set", "craw_awb_smoother_push",
 )
 
 
@@ -232,6 +260,26 @@ def _check(ret: int, what: str) -> int:
 
 
 _lib = None
+
+
+def awb_signatures() -> dict:
+    """ctypes signatures of the locus, AWB estimator and smoother functions
+    (the same in the reference's build, which the tests load beside)."""
+    vp, i32, f32, f64 = C.c_void_p, C.c_int, C.c_float, C.c_double
+    return {
+        "craw_profile_neutral_to_illuminant": (i32, [C.POINTER(Profile), f32, f32, C.POINTER(Illuminant)]),
+        "craw_profile_illuminant_to_neutral": (i32, [C.POINTER(Profile), C.POINTER(Illuminant),
+                                                     C.POINTER(f32), C.POINTER(f32)]),
+        "craw_awb_params_init": (None, [C.POINTER(AwbParams)]),
+        "craw_awb_estimate": (i32, [C.POINTER(Profile), C.POINTER(AwbHistogramC), C.POINTER(AwbParams),
+                                    C.POINTER(AwbEstimate)]),
+        "craw_awb_smoother_params_init": (None, [C.POINTER(AwbSmootherParams)]),
+        "craw_awb_smoother_create": (i32, [C.POINTER(AwbSmootherParams), C.POINTER(vp)]),
+        "craw_awb_smoother_free": (None, [C.POINTER(vp)]),
+        "craw_awb_smoother_reset": (None, [vp]),
+        "craw_awb_smoother_set": (None, [vp, f64, C.POINTER(Illuminant)]),
+        "craw_awb_smoother_push": (i32, [vp, f64, C.POINTER(AwbEstimate), C.c_bool, C.POINTER(Illuminant)]),
+    }
 
 
 def lib() -> C.CDLL:
@@ -280,6 +328,7 @@ def lib() -> C.CDLL:
         "craw_batch_free": (None, [C.POINTER(vp)]),
         "craw_awb_histogram_from_rgb_cuda_noalloc": (i32, [vp, u32, u32, C.c_size_t, i32,
                                                            C.POINTER(C.c_float * 3), vp, vp, vp, vp]),
+        **awb_signatures(),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -495,6 +544,62 @@ class Pipeline:
 
     def __exit__(self, *exc):
         self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def awb_params(**kw) -> AwbParams:
+    p = AwbParams()
+    lib().craw_awb_params_init(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def awb_estimate(profile: Profile, count: np.ndarray, weight: np.ndarray,
+                 weight_bright: np.ndarray | None, params: AwbParams | None = None,
+                 bins: int = AWB_BINS, log_min: float = -2.5, log_max: float = 1.0,
+                 library: C.CDLL | None = None) -> AwbEstimate:
+    """craw_awb_estimate over three (bins, bins) uint32 arrays."""
+    L_ = library or lib()
+    arrs = [np.ascontiguousarray(a, dtype=np.uint32) if a is not None else None
+            for a in (count, weight, weight_bright)]
+    P32 = C.POINTER(C.c_uint32)
+    h = AwbHistogramC(bins, log_min, log_max, *[a.ctypes.data_as(P32) if a is not None else P32()
+                                                for a in arrs])
+    out = AwbEstimate()
+    _check(L_.craw_awb_estimate(C.byref(profile), C.byref(h), C.byref(params) if params else None,
+                                C.byref(out)), "craw_awb_estimate")
+    return out
+
+
+class AwbSmoother:
+    """craw_awb_smoother_*: one stream's illuminant track."""
+
+    def __init__(self, params: AwbSmootherParams | None = None, library: C.CDLL | None = None):
+        self._L = library or lib()
+        self._h = C.c_void_p()
+        _check(self._L.craw_awb_smoother_create(C.byref(params) if params else None,
+                                                C.byref(self._h)), "craw_awb_smoother_create")
+
+    def push(self, pts: float, est: AwbEstimate, scene_cut: bool = False) -> tuple[int, Illuminant]:
+        out = Illuminant(-1.0, -1.0)
+        ret = self._L.craw_awb_smoother_push(self._h, pts, C.byref(est), scene_cut, C.byref(out))
+        return ret, out
+
+    def set(self, pts: float, il: Illuminant) -> None:
+        self._L.craw_awb_smoother_set(self._h, pts, C.byref(il))
+
+    def reset(self) -> None:
+        self._L.craw_awb_smoother_reset(self._h)
+
+    def close(self) -> None:
+        if self._h:
+            self._L.craw_awb_smoother_free(C.byref(self._h))
 
     def __del__(self):
         try:

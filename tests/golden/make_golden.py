@@ -150,6 +150,19 @@ def main() -> None:
                                             C.byref((C.c_float * 2)(0.3127, 0.3290)), C.byref(m9)) == 0
     out["bradford/d50_d65"] = np.array(m9[:], np.float32).reshape(3, 3)
 
+    # AWB estimator, smoother and the locus conversions they stand on
+    # (reference lib/awb.c, lib/awb_smoother.c, lib/profile.c).
+    import awb_cases as AC
+    AC.bind(ref.lib)
+    for name, cnt, wgt, brt, _ in AC.histogram_cases(ref.lib, prof):
+        out[f"awb_est/{name}/count"], out[f"awb_est/{name}/weight"] = cnt, wgt
+        if brt is not None:
+            out[f"awb_est/{name}/weight_bright"] = brt
+    out["awb_est/rows"] = AC.run_estimates(ref.lib, prof)
+    for name, params, seed_il, ev in AC.smoother_cases():
+        out[f"awb_smooth/{name}"] = AC.run_smoother(ref.lib, params, seed_il, ev)
+    out["locus/rows"] = AC.run_locus(ref.lib, prof)
+
     np.savez_compressed(HERE / "reference_outputs.npz", **out)
     print(f"wrote {HERE / 'reference_outputs.npz'} ({len(out)} arrays)")
 
