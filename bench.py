@@ -55,6 +55,8 @@ def parse():
     ap.add_argument("--impl", default="fused", choices=["fused", "plain", "reference"])
     ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16"])
     ap.add_argument("--no-extras", action="store_true", help="skip the plain/fp16/cpu side runs")
+    ap.add_argument("--extras", default="plain,fp16,batch,serve,cpu",
+                    help="comma list of side runs: plain, fp16, batch, serve, cpu")
     ap.add_argument("--width", type=int, default=5760)
     ap.add_argument("--height", type=int, default=3240)
     return ap.parse_args()
@@ -361,11 +363,14 @@ def run_gpu(args):
                   "the RGBA32F frame to pinned memory, one stream, wall clock"}
 
     extras = {}
-    if not args.no_extras and rank == 0:
+    want = set() if args.no_extras else set(args.extras.split(","))
+    if want and rank == 0:
         for name, (im, st) in {"plain_fp32": (L.IMPL_PLAIN, L.STORAGE_FP32),
                                "fused_fp16": (L.IMPL_FUSED, L.STORAGE_FP16),
                                "fused_fp32": (L.IMPL_FUSED, L.STORAGE_FP32)}.items():
             if im == impl and st == storage:
+                continue
+            if ("plain" if im == L.IMPL_PLAIN else "fp16") not in want:
                 continue
             with make_pipe(im, st, profile=False) as p2:
                 m2, _, _ = timed(p2, max(5, args.steps // 3), 3, collect=False)
@@ -373,13 +378,19 @@ def run_gpu(args):
         base = extras.get("plain_fp32", {}).get("fps")
         if base:
             extras["speedup_vs_plain_fp32"] = (args.steps / total_s) / base
-        extras["batch"] = run_batch_mix(ctx, stream, max(5, args.steps // 3), 3)
-        if base:
-            extras["batch"]["eq_speedup_vs_plain_fp32"] = (
-                extras["batch"]["fused_graph"]["eq_5760x3240_fps"] / base)
+        if "batch" in want:
+            extras["batch"] = run_batch_mix(ctx, stream, max(5, args.steps // 3), 3)
+            if base:
+                extras["batch"]["eq_speedup_vs_plain_fp32"] = (
+                    extras["batch"]["fused_graph"]["eq_5760x3240_fps"] / base)
+        if "serve" in want:
+            extras["serve"] = run_serve(ctx)
+            if base:
+                extras["serve"]["eq_speedup_vs_plain_fp32"] = (
+                    extras["serve"]["saturated"]["eq_5760x3240_fps"] / base)
 
     cpu = None
-    if rank == 0 and not args.no_extras:
+    if rank == 0 and "cpu" in want:
         cpu = cpu_oracle_fps(host_frames[0], L.pipeline_params(w, h, debayer=c.debayer, out_space=c.out_space,
                                                               flags=c.flags), fp, 1.0)
 
@@ -488,6 +499,104 @@ def run_batch_mix(ctx, stream, steps: int, warmup: int) -> dict:
     res["speedup_vs_single_frames"] = (res["fused_graph"]["frames_per_s"] /
                                        res["single_frame_pipeline"]["frames_per_s"])
     return res
+
+
+SERVE_STREAMS = ([(1920, 1080, 60.0, "clip")] * 2 + [(3840, 2160, 30.0, "clip")] * 3 +
+                 [(5760, 3240, 24.0, "clip")] * 2 + [(6000, 4000, 2.0, "stills")])
+
+
+def run_serve(ctx, seconds: float = 5.0, frames_per_clip: int = 120) -> dict:
+    """The serving workload through the frame server (craw_server_*): 8
+    streams - 2 x 1920x1080 at 60 fps, 3 x 3840x2160 at 30, 2 x 5760x3240 at
+    24 and one of 6000x4000 stills arriving as a Poisson process at 2/s -
+    admitted under a 60 GB budget; clips run temporal 0.8 + NLM 1.0 + RCD +
+    ACES AP0 float32 (stills the same without the temporal stage, each
+    still being a new scene), from pinned host memory to pinned host
+    memory. Paced: frames are submitted at their arrival times for
+    `seconds` (at most frames_per_clip per clip); latency is submission to
+    the result in host memory. Saturated: every frame of the same schedule
+    submitted at once, for the aggregate throughput."""
+    import torch
+    import libcraw_gb300 as L
+    from libcraw_gb300 import workloads as W
+
+    prof = W.make_profile()
+    rng = np.random.default_rng(5005)
+    movers = [(2.0, 0.5), (8.0, 2.0), (24.0, 10.0)]
+    streams = []
+    for k, (w, h, rate, kind) in enumerate(SERVE_STREAMS):
+        clip = kind == "clip"
+        a_dn, b_dn = float(rng.uniform(2.0, 6.0)), float(rng.uniform(20.0, 60.0))
+        src = [torch.from_numpy(W.synth_frame(w, h, 50050 + 97 * k + i, frame=i, rects=64, zone_plates=2,
+                                              noise_a_dn=a_dn, noise_b_dn=b_dn,
+                                              movers=movers if clip else []).view(np.int16)).pin_memory()
+               for i in range(4)]
+        dst = [torch.empty((h, w, 4), dtype=torch.float32).pin_memory() for _ in range(3)]
+        kw = dict(denoise_strength=1.0, noise_override=W.noise_model(a_dn, b_dn))
+        if clip:
+            kw["denoise_temporal_strength"] = 0.8
+        flags = L.FLAG_DENOISE | (L.FLAG_TEMPORAL_DENOISE if clip else 0)
+        pp = L.pipeline_params(w, h, debayer=L.DEBAYER_RCD, out_space=L.CS_ACES_AP0, flags=flags,
+                               out_format=L.FORMAT_RGBA32F)
+        if clip:
+            times = [i / rate for i in range(min(frames_per_clip, int(seconds * rate)))]
+        else:
+            times, t = [], float(rng.exponential(1.0 / rate))
+            while t < seconds:
+                times.append(t)
+                t += float(rng.exponential(1.0 / rate))
+        streams.append(dict(w=w, h=h, rate=rate, kind=kind, src=src, dst=dst,
+                            fp=L.frame_params(prof, **kw), pp=pp, times=times))
+
+    def run(paced: bool) -> dict:
+        with L.Server(ctx, L.server_params(hbm_budget=60 << 30, max_inflight=16,
+                                           slots_per_stream=2)) as srv:
+            for s in streams:
+                s["sid"] = srv.open(L.server_stream_params(s["pp"]))
+            resident = srv.stats().hbm_resident
+            sched = sorted((t, k, i) for k, s in enumerate(streams) for i, t in enumerate(s["times"]))
+            res = []
+            t0 = time.perf_counter()
+            for t, k, i in sched:
+                if paced:
+                    while time.perf_counter() - t0 < t:
+                        res += srv.poll(64, 0)
+                        time.sleep(0.0002)
+                s = streams[k]
+                srcb, dstb = s["src"][i % 4], s["dst"][i % 3]
+                srv.submit(s["sid"], srcb.data_ptr(), s["w"] * 2, dstb.data_ptr(), s["w"] * 16,
+                           s["fp"], t, (k << 32) | i)
+            srv.drain()
+            wall = time.perf_counter() - t0
+            while True:
+                got = srv.poll(256, 0)
+                if not got:
+                    break
+                res += got
+            st = srv.stats()
+        lat = np.array([r.latency_ms for r in res])
+        px = sum(streams[r.user >> 32]["w"] * streams[r.user >> 32]["h"] for r in res)
+        out = {"frames": len(res), "failed": int(st.failed), "wall_s": wall,
+               "fps": len(res) / wall, "eq_5760x3240_fps": px / (5760 * 3240) / wall,
+               "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+               "max_ms": float(lat.max()), "hbm_resident_gb": resident / 1e9,
+               "device_ms_mean": float(np.mean([r.device_ms for r in res]))}
+        per = {}
+        for k, s in enumerate(streams):
+            key = f"{s['w']}x{s['h']}@{s['rate']:g}"
+            lk = [r.latency_ms for r in res if r.user >> 32 == k]
+            per.setdefault(key, []).extend(lk)
+        out["per_class"] = {k: {"frames": len(v), "p50_ms": float(np.percentile(v, 50)),
+                                "p99_ms": float(np.percentile(v, 99))} for k, v in per.items() if v}
+        return out
+
+    paced = run(True)
+    saturated = run(False)
+    return {"workload": "8 streams: 2x1920x1080@60, 3x3840x2160@30, 2x5760x3240@24 (temporal 0.8 + "
+                        "NLM 1.0 + RCD + ACES AP0 f32), 1x6000x4000 stills Poisson 2/s (NLM + RCD + "
+                        "AP0); pinned host in and out; 60 GB budget",
+            "seconds": seconds, "paced": paced, "saturated": saturated,
+            "p99_under_60fps_interval": paced["p99_ms"] < 1000.0 / 60}
 
 
 def main():

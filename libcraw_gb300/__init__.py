@@ -203,6 +203,33 @@ class AwbSmootherParams(C.Structure):
                 ("max_slew_mired_per_s", C.c_float), ("min_confidence", C.c_float)]
 
 
+class ServerParams(C.Structure):
+    _fields_ = [("hbm_budget", C.c_uint64), ("max_inflight", C.c_uint32),
+                ("slots_per_stream", C.c_uint32), ("idle_timeout_ms", C.c_uint32),
+                ("padding", C.c_uint8 * 44)]
+
+
+class ServerStreamParams(C.Structure):
+    _fields_ = [("pipeline", PipelineParams), ("flags", C.c_uint32), ("awb", AwbParams),
+                ("smoother", AwbSmootherParams), ("padding", C.c_uint8 * 64)]
+
+
+class ServerResult(C.Structure):
+    _fields_ = [("user", C.c_uint64), ("stream", C.c_uint32), ("status", C.c_int),
+                ("queue_ms", C.c_double), ("latency_ms", C.c_double), ("device_ms", C.c_double),
+                ("awb_valid", C.c_bool), ("awb", Illuminant), ("estimate", AwbEstimate)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("hbm_budget", C.c_uint64), ("hbm_resident", C.c_uint64), ("streams", C.c_uint32),
+                ("queued", C.c_uint32), ("inflight", C.c_uint32), ("submitted", C.c_uint64),
+                ("completed", C.c_uint64), ("failed", C.c_uint64), ("streams_admitted", C.c_uint64),
+                ("streams_refused", C.c_uint64), ("streams_reclaimed", C.c_uint64)]
+
+
+SERVER_STREAM_AUTO_WB = 1 << 0
+
+
 class BatchParams(C.Structure):
     _fields_ = [("max_frames", C.c_uint32), ("max_width", C.c_uint32), ("max_height", C.c_uint32),
                 ("debayer", C.c_int), ("out_space", C.c_int), ("out_format", C.c_int),
@@ -216,7 +243,8 @@ class BatchInfo(C.Structure):
 
 for _s, _n in ((Profile, 1264), (FrameParams, 264), (PipelineParams, 256), (CudaInitParams, 64),
                (ContextOptions, 1024), (LensCorrection, 64), (BatchParams, 64), (AwbParams, 36),
-               (AwbCandidate, 20), (AwbEstimate, 68), (AwbSmootherParams, 16)):
+               (AwbCandidate, 20), (AwbEstimate, 68), (AwbSmootherParams, 16), (ServerParams, 64),
+               (ServerStreamParams, 376), (ServerResult, 120)):
     assert C.sizeof(_s) == _n, (_s.__name__, C.sizeof(_s), _n)
 
 # ----------------------------------------------------------------- library
@@ -240,6 +268,9 @@ EXPORTS = (
     "craw_awb_params_init", "craw_awb_estimate", "craw_awb_smoother_params_init",
     "craw_awb_smoother_create", "craw_awb_smoother_free", "craw_awb_smoother_reset",
     "craw_awb_smoother_set", "craw_awb_smoother_push",
+    "craw_server_params_init", "craw_server_stream_params_init", "craw_server_create",
+    "craw_server_free", "craw_server_stream_open", "craw_server_stream_close",
+    "craw_server_submit", "craw_server_poll", "craw_server_drain", "craw_server_get_stats",
 )
 
 
@@ -329,6 +360,17 @@ def lib() -> C.CDLL:
         "craw_awb_histogram_from_rgb_cuda_noalloc": (i32, [vp, u32, u32, C.c_size_t, i32,
                                                            C.POINTER(C.c_float * 3), vp, vp, vp, vp]),
         **awb_signatures(),
+        "craw_server_params_init": (None, [C.POINTER(ServerParams)]),
+        "craw_server_stream_params_init": (None, [C.POINTER(ServerStreamParams)]),
+        "craw_server_create": (i32, [vp, C.POINTER(ServerParams), C.POINTER(vp)]),
+        "craw_server_free": (None, [C.POINTER(vp)]),
+        "craw_server_stream_open": (i32, [vp, C.POINTER(ServerStreamParams), C.POINTER(u32)]),
+        "craw_server_stream_close": (i32, [vp, u32]),
+        "craw_server_submit": (i32, [vp, u32, vp, C.c_size_t, vp, C.c_size_t, C.POINTER(FrameParams),
+                                     C.c_double, C.c_uint64]),
+        "craw_server_poll": (i32, [vp, C.POINTER(ServerResult), u32, i32]),
+        "craw_server_drain": (i32, [vp]),
+        "craw_server_get_stats": (i32, [vp, C.POINTER(ServerStats)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -600,6 +642,76 @@ class AwbSmoother:
     def close(self) -> None:
         if self._h:
             self._L.craw_awb_smoother_free(C.byref(self._h))
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def server_params(**kw) -> ServerParams:
+    p = ServerParams()
+    lib().craw_server_params_init(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def server_stream_params(pipeline: PipelineParams, flags: int = 0) -> ServerStreamParams:
+    p = ServerStreamParams()
+    lib().craw_server_stream_params_init(C.byref(p))
+    p.pipeline = pipeline
+    p.flags = flags
+    return p
+
+
+class Server:
+    """craw_server_*: streams admitted under a device-memory budget, frames
+    from host memory developed as they arrive."""
+
+    def __init__(self, ctx: Context, params: ServerParams):
+        self.ctx = ctx
+        self._h = C.c_void_p()
+        _check(lib().craw_server_create(ctx.handle, C.byref(params), C.byref(self._h)),
+               "craw_server_create")
+
+    def open(self, params: ServerStreamParams) -> int:
+        sid = C.c_uint32()
+        _check(lib().craw_server_stream_open(self._h, C.byref(params), C.byref(sid)),
+               "craw_server_stream_open")
+        return sid.value
+
+    def close_stream(self, sid: int) -> None:
+        _check(lib().craw_server_stream_close(self._h, sid), "craw_server_stream_close")
+
+    def submit(self, sid: int, src: int, src_pitch: int, dst: int, dst_pitch: int,
+               fp: FrameParams, pts: float = 0.0, user: int = 0) -> None:
+        _check(lib().craw_server_submit(self._h, sid, C.c_void_p(src), src_pitch, C.c_void_p(dst),
+                                        dst_pitch, C.byref(fp), pts, user), "craw_server_submit")
+
+    def poll(self, max_results: int = 64, timeout_ms: int = 0) -> list[ServerResult]:
+        buf = (ServerResult * max_results)()
+        n = _check(lib().craw_server_poll(self._h, buf, max_results, timeout_ms), "craw_server_poll")
+        return [buf[i] for i in range(n)]
+
+    def drain(self) -> None:
+        _check(lib().craw_server_drain(self._h), "craw_server_drain")
+
+    def stats(self) -> ServerStats:
+        st = ServerStats()
+        _check(lib().craw_server_get_stats(self._h, C.byref(st)), "craw_server_get_stats")
+        return st
+
+    def close(self) -> None:
+        if self._h:
+            lib().craw_server_free(C.byref(self._h))
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
     def __del__(self):
         try:
