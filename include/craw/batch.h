@@ -6,8 +6,9 @@
  * in one persistent launch: every denoise tile of every frame, a
  * grid-wide barrier, every develop tile of every frame. The launch is
  * captured into a CUDA graph the first time a set of frame shapes is seen
- * and replayed for every later recording with the same shapes; only the
- * per-frame constants (a small table) are copied before each replay.
+ * and replayed for every later recording with the same shapes; each
+ * replay gets the recording's per-frame constants as new parameters of
+ * the captured kernel nodes (the table travels with the launch).
  * Frames of a batch have no temporal history and no AWB histogram.
  */
 #ifndef CRAW_BATCH_H

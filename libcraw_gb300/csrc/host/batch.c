@@ -22,10 +22,7 @@ struct CRAWBatch {
     bool fused, use_graph, denoise;
     uint16_t *clean[BATCH_MAX];
     size_t clean_pitch;
-    CRAWKBatchFrame *table_dev;
-    CRAWKBatchFrame *table_host[2];
-    cudaEvent_t table_done[2];
-    int table_slot;
+    CRAWKBatchTable *table;          /* host; each launch carries a copy */
     cudaStream_t cap_stream;
     cudaGraph_t graph;
     cudaGraphExec_t exec;
@@ -58,14 +55,8 @@ static void batch_release(CRAWBatch *b)
         cudaGraphDestroy(b->graph);
     for (uint32_t i = 0; i < BATCH_MAX; i++)
         craw_dev_free(ctx, b->clean[i]);
-    craw_dev_free(ctx, b->table_dev);
     craw_dev_sync(ctx);
-    for (int i = 0; i < 2; i++) {
-        if (b->table_done[i])
-            cudaEventDestroy(b->table_done[i]);
-        if (b->table_host[i])
-            cudaFreeHost(b->table_host[i]);
-    }
+    free(b->table);
     if (b->cap_stream)
         cudaStreamDestroy(b->cap_stream);
     free(b);
@@ -96,7 +87,7 @@ static int batch_autotune(CRAWBatch *b)
 {
     CRAWContext *ctx = b->ctx;
     const uint32_t w = b->params.max_width, h = b->params.max_height;
-    CRAWKBatchFrame *F = b->table_host[0];
+    CRAWKBatchFrame *F = &b->table->f[0];
     void *out = NULL;
     uint16_t *mosaic;
     size_t out_pitch = (((size_t)w * 16) + 255) / 256 * 256;
@@ -147,13 +138,9 @@ static int batch_autotune(CRAWBatch *b)
         F->vio.dst = out;
         F->vio.dst_pitch = out_pitch;
         batch_layout(b, 1, &w, &h, &dn, F, &dn_items, &dv_items);
-        if (cudaMemcpyAsync(b->table_dev, F, sizeof(*F), cudaMemcpyHostToDevice, ctx->stream) != cudaSuccess) {
-            ret = CRAW_ERROR(EIO);
-            goto done;
-        }
         for (int r = 0; r < 3; r++) {
             cudaEventRecord(e0, ctx->stream);
-            if (craw_k_batch(b->table_dev, 1, dn_items, dv_items, b->params.debayer, shape, b->fused,
+            if (craw_k_batch(b->table, 1, dn_items, dv_items, b->params.debayer, shape, b->fused,
                              ctx->stream) < 0) {
                 ret = CRAW_ERROR(EIO);
                 goto done;
@@ -221,16 +208,9 @@ CRAW_API int craw_batch_create(CRAWContext *ctx, const CRAWBatchParams *params, 
     for (uint32_t i = 0; i < params->max_frames; i++)
         if ((ret = craw_dev_alloc(ctx, (void **)&b->clean[i], b->clean_pitch * params->max_height)) < 0)
             goto fail;
-    if ((ret = craw_dev_alloc(ctx, (void **)&b->table_dev,
-                              params->max_frames * sizeof(CRAWKBatchFrame))) < 0)
+    if (!(b->table = calloc(1, sizeof(*b->table)))) {
+        ret = CRAW_ERROR(ENOMEM);
         goto fail;
-    for (int i = 0; i < 2; i++) {
-        if (cudaHostAlloc((void **)&b->table_host[i], params->max_frames * sizeof(CRAWKBatchFrame),
-                          cudaHostAllocDefault) != cudaSuccess ||
-            cudaEventCreateWithFlags(&b->table_done[i], cudaEventDisableTiming) != cudaSuccess) {
-            ret = CRAW_ERROR(ENOMEM);
-            goto fail;
-        }
     }
     if (cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
         ret = CRAW_ERROR(ENOMEM);
@@ -277,7 +257,7 @@ static int batch_capture(CRAWBatch *b, uint32_t nb, int32_t dn_items, int32_t dv
 
     if (cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
         return CRAW_ERROR(EIO);
-    ret = craw_k_batch(b->table_dev, (int32_t)nb, dn_items, dv_items, b->params.debayer, b->shape,
+    ret = craw_k_batch(b->table, (int32_t)nb, dn_items, dv_items, b->params.debayer, b->shape,
                        b->fused, b->cap_stream);
     if (cudaStreamEndCapture(b->cap_stream, &g) != cudaSuccess || ret < 0) {
         if (g)
@@ -318,12 +298,9 @@ CRAW_API int craw_batch_record(CRAWBatch *b, cudaStream_t s, uint32_t nb, const 
         craw_log(ctx, CRAW_LOG_ERROR, "%u frames; the batch holds %u\n", nb, b->params.max_frames);
         return CRAW_ERROR(EINVAL);
     }
-    /* The host table this recording fills was last copied two recordings
-     * ago; that copy has long been issued, wait for it to finish. */
-    b->table_slot ^= 1;
-    F = b->table_host[b->table_slot];
-    if (cudaEventSynchronize(b->table_done[b->table_slot]) != cudaSuccess)
-        return CRAW_ERROR(EIO);
+    /* Each launch carries its own copy of the table (a kernel parameter),
+     * so the host table is free again as soon as the launch is enqueued. */
+    F = b->table->f;
     memset(F, 0, nb * sizeof(*F));
     for (uint32_t i = 0; i < nb; i++) {
         w[i] = src[i].width;
@@ -382,14 +359,15 @@ CRAW_API int craw_batch_record(CRAWBatch *b, cudaStream_t s, uint32_t nb, const 
         b->sig_dn_items = dn_items;
         b->sig_dv_items = dv_items;
     }
-    if (cudaMemcpyAsync(b->table_dev, F, nb * sizeof(*F), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-        cudaEventRecord(b->table_done[b->table_slot], s) != cudaSuccess)
-        return CRAW_ERROR(EIO);
     if (b->use_graph) {
-        if (cudaGraphLaunch(b->exec, s) != cudaSuccess)
+        /* The captured nodes get this recording's table and counts. */
+        if (craw_k_batch_update(b->exec, b->graph, b->table, (int32_t)nb, dn_items, dv_items) < 0 ||
+            cudaGraphLaunch(b->exec, s) != cudaSuccess) {
+            (void)cudaGetLastError();
             return CRAW_ERROR(EIO);
+        }
         b->replays++;
-    } else if (craw_k_batch(b->table_dev, (int32_t)nb, dn_items, dv_items, b->params.debayer, b->shape,
+    } else if (craw_k_batch(b->table, (int32_t)nb, dn_items, dv_items, b->params.debayer, b->shape,
                             b->fused, s) < 0) {
         return CRAW_ERROR(EIO);
     }

@@ -163,13 +163,26 @@ enum CRAWKBatchShape {
 void craw_k_batch_tiles(int32_t w, int32_t h, int shape, int32_t *dn_tx, int32_t *dn_ty,
                         int32_t *dv_tx, int32_t *dv_ty);
 
-/* Develops the `nb` frames of the table `frames` (device memory) in one
- * persistent launch: every denoise tile of every frame, a grid-wide
- * barrier, every develop tile (`fused`); or as two persistent launches.
- * Grid: as many CTAs as fit on the device at once. All frames use the
- * same debayer, RCD or MHC or bilinear, `method`. */
-int craw_k_batch(const CRAWKBatchFrame *frames, int32_t nb, int32_t dn_items, int32_t dv_items,
+/* The frames of one batch launch, passed by value as a kernel parameter
+ * (30 KB of the 32 KB a launch may carry): the kernels read a frame's
+ * constants from the parameter bank, not from memory they must copy. */
+#define CRAW_K_BATCH_MAX 64
+typedef struct CRAWKBatchTable {
+    CRAWKBatchFrame f[CRAW_K_BATCH_MAX];
+} CRAWKBatchTable;
+
+/* Develops the first `nb` frames of `table` (host memory, copied into the
+ * launch) in one persistent launch: every denoise tile of every frame, a
+ * grid-wide barrier, every develop tile (`fused`); or as two persistent
+ * launches. Grid: as many CTAs as fit on the device at once. All frames
+ * use the same debayer, RCD or MHC or bilinear, `method`. */
+int craw_k_batch(const CRAWKBatchTable *table, int32_t nb, int32_t dn_items, int32_t dv_items,
                  int method, int shape, int fused, cudaStream_t s);
+
+/* Points every batch kernel node of an instantiated graph (one captured
+ * craw_k_batch call) at a new table and item counts. */
+int craw_k_batch_update(cudaGraphExec_t exec, cudaGraph_t graph, const CRAWKBatchTable *table,
+                        int32_t nb, int32_t dn_items, int32_t dv_items);
 
 /* ------------------------------------------------------- plain baseline */
 
