@@ -45,6 +45,8 @@ import numpy as np  # noqa: E402
 
 METRIC = "5760x3240 frames/s full develop; p50/p99 frame latency at <=1e-3 rel err"
 WORKLOAD = "5760x3240 RGGB 12-bit: VST + NLM 1.0 + RCD + ACES AP1 (RGC) float32 + AWB histogram"
+#: Denoise tile shapes by craw_pipeline_get_kernel_config() index.
+DN_SHAPES = ["2x8", "2x4", "2x8 f32x2", "2x4 f32x2"]
 
 
 def parse():
@@ -55,8 +57,8 @@ def parse():
     ap.add_argument("--impl", default="fused", choices=["fused", "plain", "reference"])
     ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16"])
     ap.add_argument("--no-extras", action="store_true", help="skip the plain/fp16/cpu side runs")
-    ap.add_argument("--extras", default="plain,fp16,batch,serve,cpu",
-                    help="comma list of side runs: plain, fp16, batch, serve, cpu")
+    ap.add_argument("--extras", default="plain,fp16,batch,temporal,serve,cpu",
+                    help="comma list of side runs: plain, fp16, batch, temporal, serve, cpu")
     ap.add_argument("--width", type=int, default=5760)
     ap.add_argument("--height", type=int, default=3240)
     return ap.parse_args()
@@ -337,30 +339,50 @@ def run_gpu(args):
                                "peak = SMs x 128 FP32 lanes x median SM clock"}
 
     # End to end through the same call: pinned host mosaic in, RGBA32F out.
+    # Three lanes (pipeline + CUDA stream + device buffers each) take the
+    # steps in turn, so one frame's copy in, another's kernels and a third's
+    # copy out overlap, as a caller streaming frames would arrange it.
     pinned_in = [torch.from_numpy(f.view(np.int16)).pin_memory() for f in host_frames]
-    pinned_out = torch.empty((h, w, 4), dtype=torch.float32).pin_memory()
-    dev_in = torch.empty((h, w), dtype=torch.int16, device="cuda")
-    src_e = L.Image(dev_in.data_ptr(), w * 2, L.FORMAT_R16_UNORM, w, h)
-    e2e_pipe = make_pipe(impl, storage, profile=False)
-    with torch.cuda.stream(stream):
-        for i in range(3):
-            dev_in.copy_(pinned_in[i % nfr], non_blocking=True)
-            e2e_pipe.record(sptr, src_e, dst, fp)
-            pinned_out.copy_(out, non_blocking=True)
+    lanes = []
+    for _ in range(3):
+        ls = torch.cuda.Stream()
+        d_in = torch.empty((h, w), dtype=torch.int16, device="cuda")
+        d_out = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+        lanes.append(dict(stream=ls, d_in=d_in, d_out=d_out,
+                          h_out=torch.empty((h, w, 4), dtype=torch.float32).pin_memory(),
+                          src=L.Image(d_in.data_ptr(), w * 2, L.FORMAT_R16_UNORM, w, h),
+                          dst=L.Image(d_out.data_ptr(), w * 16, L.FORMAT_RGBA32F, w, h),
+                          pipe=make_pipe(impl, storage, profile=False)))
+
+    def e2e_step(i, nl):
+        ln = lanes[i % nl]
+        with torch.cuda.stream(ln["stream"]):
+            ln["d_in"].copy_(pinned_in[i % nfr], non_blocking=True)
+            ln["pipe"].record(ln["stream"].cuda_stream, ln["src"], ln["dst"], fp)
+            ln["h_out"].copy_(ln["d_out"], non_blocking=True)
+
+    def e2e_run(nl):
+        for i in range(3 * nl):
+            e2e_step(i, nl)
         torch.cuda.synchronize()
         barrier(ws)
         t0 = time.perf_counter()
         for i in range(args.steps):
-            dev_in.copy_(pinned_in[i % nfr], non_blocking=True)
-            e2e_pipe.record(sptr, src_e, dst, fp)
-            pinned_out.copy_(out, non_blocking=True)
+            e2e_step(i, nl)
         torch.cuda.synchronize()
-        e2e_s = time.perf_counter() - t0
-    e2e_s = max_over_ranks(e2e_s, ws)
+        return max_over_ranks(time.perf_counter() - t0, ws)
+
+    e2e_s1 = e2e_run(1)
+    e2e_s = e2e_run(len(lanes))
     e2e = {"value": ws * args.steps / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": w * h * 2,
            "d2h_bytes_per_step": w * h * 16,
+           "one_stream_value": ws * args.steps / e2e_s1,
            "how": "per step: H2D of the mosaic from pinned memory, craw_pipeline_record, D2H of "
-                  "the RGBA32F frame to pinned memory, one stream, wall clock"}
+                  "the RGBA32F frame to pinned memory, on one of 3 streams in turn (each with its "
+                  "own pipeline and buffers); wall clock over all steps; one_stream_value: all "
+                  "steps on one stream"}
+    for ln in lanes:
+        ln["pipe"].close()
 
     extras = {}
     want = set() if args.no_extras else set(args.extras.split(","))
@@ -383,6 +405,8 @@ def run_gpu(args):
             if base:
                 extras["batch"]["eq_speedup_vs_plain_fp32"] = (
                     extras["batch"]["fused_graph"]["eq_5760x3240_fps"] / base)
+        if "temporal" in want:
+            extras["temporal_seq"] = run_temporal_seq(ctx, stream)
         if "serve" in want:
             extras["serve"] = run_serve(ctx)
             if base:
@@ -405,7 +429,7 @@ def run_gpu(args):
             "config": {"workload": WORKLOAD, "width": w, "height": h, "impl": args.impl,
                        "storage": args.storage, "l2": "flushed between steps (256 MB write)",
                        "parallelism": f"replicas x{ws}",
-                       "denoise_tile": ["2x8", "2x4"][kcfg[0]] + " (autotuned)"},
+                       "denoise_tile": DN_SHAPES[kcfg[0]] + " (autotuned)"},
             "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
                            "max": lat[-1]},
             "stage_ms": {k: statistics.mean(v) for k, v in stage.items()},
@@ -423,7 +447,6 @@ def run_gpu(args):
         }
         print(json.dumps(line), flush=True)
     pipe.close()
-    e2e_pipe.close()
     ctx.close()
     if ws > 1:
         import torch.distributed as dist
@@ -498,6 +521,61 @@ def run_batch_mix(ctx, stream, steps: int, warmup: int) -> dict:
         p_.close()
     res["speedup_vs_single_frames"] = (res["fused_graph"]["frames_per_s"] /
                                        res["single_frame_pipeline"]["frames_per_s"])
+    return res
+
+
+def run_temporal_seq(ctx, stream, nsteps: int = 60, distinct: int = 12) -> dict:
+    """The temporal sequence (60 frames of 5760x3240, rectangles moving 2, 8
+    and 24 px/frame, temporal 0.8 + NLM 1.0 + chroma 0.5 + MHC + P3-D65
+    float32 + AWB) through one pipeline, FP32 and FP16 storage: frames/s
+    from CUDA events around each record, and how far the FP16 output lies
+    from the FP32 one on the last frame. `distinct` seeded frames are
+    generated and cycled (the work does not depend on the content)."""
+    import torch
+    import libcraw_gb300 as L
+    from libcraw_gb300 import workloads as W
+
+    c = W.config(3)
+    w, h = c.width, c.height
+    prof = W.make_profile()
+    fp = L.frame_params(prof, **c.frame_kwargs())
+    dev = [torch.from_numpy(c.frame(i).view(np.int16)).cuda() for i in range(distinct)]
+    srcs = [L.Image(t.data_ptr(), w * 2, L.FORMAT_R16_UNORM, w, h) for t in dev]
+    out = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    dst = L.Image(out.data_ptr(), w * 16, L.FORMAT_RGBA32F, w, h)
+    sptr = stream.cuda_stream
+    res, last = {}, {}
+    for name, storage in (("fp32", L.STORAGE_FP32), ("fp16", L.STORAGE_FP16)):
+        pp = L.pipeline_params(w, h, debayer=c.debayer, out_space=c.out_space,
+                               flags=c.flags | L.FLAG_PROFILE, out_format=L.FORMAT_RGBA32F,
+                               storage=storage, nb_awb_slots=2)
+        with L.Pipeline(ctx, pp) as pipe, torch.cuda.stream(stream):
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(nsteps)]
+            stage: dict[str, list[float]] = {}
+            for i, (e0, e1) in enumerate(evs):
+                e0.record(stream)
+                pipe.record(sptr, srcs[i % distinct], dst, fp)
+                e1.record(stream)
+                if i >= 3:
+                    e1.synchronize()
+                    for sname, _, ms in pipe.stage_times():
+                        stage.setdefault(sname, []).append(ms)
+            torch.cuda.synchronize()
+            last[name] = out.clone()
+        ms = sorted(a.elapsed_time(b) for a, b in evs[3:])
+        res[name] = {"fps": 1000.0 * len(ms) / sum(ms), "p50_ms": ms[len(ms) // 2],
+                     "p99_ms": ms[min(len(ms) - 1, int(0.99 * len(ms)))],
+                     "stage_ms": {k: statistics.mean(v) for k, v in stage.items()}}
+    a, b = last["fp16"].float(), last["fp32"].float()
+    peak = float(b[..., :3].abs().max())
+    den = torch.maximum(b[..., :3].abs(), torch.tensor(0.01 * peak, device=b.device))
+    rel = ((a[..., :3] - b[..., :3]).abs() / den)
+    mse = float(((a[..., :3] - b[..., :3]) ** 2).mean())
+    res["fp16_vs_fp32_last_frame"] = {"max_rel": float(rel.max()), "mean_rel": float(rel.mean()),
+                                      "psnr_db": 10 * np.log10(peak * peak / max(mse, 1e-30))}
+    res["workload"] = (f"{w}x{h} x{nsteps} (12 distinct seeded frames cycled), movers 2/8/24 px: "
+                       "temporal 0.8 + NLM 1.0 + chroma 0.5 + MHC + P3-D65 f32 + AWB")
     return res
 
 
