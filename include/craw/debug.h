@@ -11,4 +11,10 @@
  * craw_pipeline_create() leaves nothing behind; 0 disarms it. */
 CRAW_API void craw_debug_fail_alloc(int k);
 
+/* Makes every pipeline created from now use denoise tile shape `shape`
+ * (the index craw_pipeline_get_kernel_config() reports) instead of the
+ * autotuner's pick, so that tests can check each shape; -1 restores the
+ * autotuner. Returns CRAW_ERROR(EINVAL) for an unknown shape. */
+CRAW_API int craw_debug_force_denoise_shape(int shape);
+
 #endif /* CRAW_DEBUG_H */

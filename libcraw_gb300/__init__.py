@@ -252,7 +252,7 @@ for _s, _n in ((Profile, 1264), (FrameParams, 264), (PipelineParams, 256), (Cuda
 #: Every symbol the C ABI exports (include/craw/*.h).
 EXPORTS = (
     "craw_version_int", "craw_log", "craw_context_create", "craw_context_free",
-    "craw_cuda_check_device", "craw_debug_fail_alloc",
+    "craw_cuda_check_device", "craw_debug_fail_alloc", "craw_debug_force_denoise_shape",
     "craw_pipeline_params_init", "craw_frame_params_init", "craw_pipeline_create",
     "craw_pipeline_free", "craw_pipeline_record", "craw_pipeline_get_awb_histogram",
     "craw_pipeline_get_awb_histogram_n", "craw_pipeline_get_stage_times",
@@ -330,6 +330,7 @@ def lib() -> C.CDLL:
         "craw_context_free": (None, [C.POINTER(vp)]),
         "craw_cuda_check_device": (i32, [i32, C.POINTER(C.c_char_p)]),
         "craw_debug_fail_alloc": (None, [i32]),
+        "craw_debug_force_denoise_shape": (i32, [i32]),
         "craw_pipeline_params_init": (None, [C.POINTER(PipelineParams)]),
         "craw_frame_params_init": (None, [C.POINTER(FrameParams)]),
         "craw_pipeline_create": (i32, [vp, C.POINTER(PipelineParams), C.POINTER(vp)]),
@@ -772,3 +773,13 @@ class Batch:
 
 def debug_fail_alloc(k: int) -> None:
     lib().craw_debug_fail_alloc(k)
+
+
+#: Denoise tile shapes by craw_pipeline_get_kernel_config() index.
+DN_SHAPES = ("2x8", "2x4", "2x8 f32x2", "2x4 f32x2")
+
+
+def debug_force_denoise_shape(shape: int) -> None:
+    """Every pipeline created from now uses denoise shape `shape` (-1: the
+    autotuner's)."""
+    _check(lib().craw_debug_force_denoise_shape(shape), "craw_debug_force_denoise_shape")

@@ -155,6 +155,16 @@ CRAW_API void craw_context_free(CRAWContext **pctx)
  * rest of the library. */
 static int craw_fail_countdown;
 
+int craw_forced_denoise_shape = -1;
+
+CRAW_API int craw_debug_force_denoise_shape(int shape)
+{
+    if (shape < -1 || shape >= CRAW_K_DN_SHAPE_NB)
+        return CRAW_ERROR(EINVAL);
+    craw_forced_denoise_shape = shape;
+    return 0;
+}
+
 CRAW_API void craw_debug_fail_alloc(int k)
 {
     craw_fail_countdown = k;

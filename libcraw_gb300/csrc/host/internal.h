@@ -37,6 +37,9 @@ int craw_dev_alloc(CRAWContext *ctx, void **ptr, size_t bytes);
 void craw_dev_free(CRAWContext *ctx, void *ptr);
 int craw_dev_sync(CRAWContext *ctx);
 
+/* craw_debug_force_denoise_shape(): -1, or the shape every new pipeline uses. */
+extern int craw_forced_denoise_shape;
+
 /* Per-frame constants (frame.c). */
 int craw_image_check(CRAWContext *ctx, const CRAWImage *img, CRAWFormat fmt, uint32_t w, uint32_t h,
                      const char *what);

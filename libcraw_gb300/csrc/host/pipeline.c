@@ -427,9 +427,12 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
     }
     if ((ret = craw_dev_sync(ctx)) < 0)
         goto fail;
-    if ((p->has_denoise || p->has_temporal) && !p->plain &&
-        !(params->flags & CRAW_PIPELINE_FLAG_NO_AUTOTUNE) && (ret = autotune(p)) < 0)
+    if (craw_forced_denoise_shape >= 0) {
+        p->dn_shape[0] = p->dn_shape[1] = craw_forced_denoise_shape;
+    } else if ((p->has_denoise || p->has_temporal) && !p->plain &&
+               !(params->flags & CRAW_PIPELINE_FLAG_NO_AUTOTUNE) && (ret = autotune(p)) < 0) {
         goto fail;
+    }
     craw_log(ctx, CRAW_LOG_VERBOSE, "pipeline %ux%u debayer %d flags 0x%x storage %s impl %s\n",
              w, h, params->debayer, params->flags, p->fp16 ? "fp16" : "fp32",
              p->plain ? "plain" : "fused");

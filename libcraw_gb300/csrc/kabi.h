@@ -46,6 +46,8 @@ typedef struct CRAWKDenoiseIO {
 enum CRAWKDenoiseShape {
     CRAW_K_DN_SHAPE_2x8 = 0,     /* a thread filters 2 columns x 8 rows */
     CRAW_K_DN_SHAPE_2x4,         /* 2 columns x 4 rows */
+    CRAW_K_DN_SHAPE_2x8_X2,      /* 2x8 with the packed f32x2 search (no history) */
+    CRAW_K_DN_SHAPE_2x4_X2,      /* 2x4 with the packed f32x2 search (no history) */
     CRAW_K_DN_SHAPE_NB,
 };
 

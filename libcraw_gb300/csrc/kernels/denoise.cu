@@ -11,19 +11,19 @@ namespace {
 
 using namespace craw_dn;
 
-template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY>
+template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2>
 __global__ void __launch_bounds__(Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>::NT)
 k_denoise(const CRAWKDenoise k, const CRAWKDenoiseIO io)
 {
     extern __shared__ __align__(16) float smem[];
-    denoise_tile<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>(k, io, blockIdx.x, blockIdx.y, smem);
+    denoise_tile<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2>(k, io, blockIdx.x, blockIdx.y, smem);
 }
 
-template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY>
+template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2>
 int launch(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, cudaStream_t s)
 {
-    using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>;
-    auto fn = k_denoise<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>;
+    using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2>;
+    auto fn = k_denoise<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2>;
     const size_t smem = (size_t)C::smem_floats * sizeof(float);
     static bool attr_set = false;   /* per process; the attribute is per function */
     if (!attr_set) {
@@ -36,16 +36,18 @@ int launch(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, cudaStream_t s)
     return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }
 
-template <int BW, int M, int WP>
+/* X2: the packed search where there is no history; with a history the
+ * shape runs the scalar search (the packed one has no history form). */
+template <int BW, int M, int WP, bool X2>
 int dispatch(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, cudaStream_t s)
 {
     const bool sp = k->mode & CRAW_K_DN_SPATIAL, te = k->mode & CRAW_K_DN_TEMPORAL;
     const bool hi = te && (k->mode & CRAW_K_DN_HISTORY);
-    if (sp && !te)  return launch<BW, M, WP, true, false, false>(k, io, s);
-    if (sp && !hi)  return launch<BW, M, WP, true, true, false>(k, io, s);
-    if (sp)         return launch<BW, M, WP, true, true, true>(k, io, s);
-    if (te && !hi)  return launch<BW, M, WP, false, true, false>(k, io, s);
-    if (te)         return launch<BW, M, WP, false, true, true>(k, io, s);
+    if (sp && !te)  return launch<BW, M, WP, true, false, false, X2>(k, io, s);
+    if (sp && !hi)  return launch<BW, M, WP, true, true, false, X2>(k, io, s);
+    if (sp)         return launch<BW, M, WP, true, true, true, false>(k, io, s);
+    if (te && !hi)  return launch<BW, M, WP, false, true, false, false>(k, io, s);
+    if (te)         return launch<BW, M, WP, false, true, true, false>(k, io, s);
     return -22;
 }
 
@@ -56,8 +58,10 @@ extern "C" int craw_k_denoise(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, i
 {
     (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
     switch (shape) {
-    case CRAW_K_DN_SHAPE_2x8: return dispatch<2, 8, 1>(k, io, s);
-    case CRAW_K_DN_SHAPE_2x4: return dispatch<2, 4, 2>(k, io, s);
+    case CRAW_K_DN_SHAPE_2x8:    return dispatch<2, 8, 1, false>(k, io, s);
+    case CRAW_K_DN_SHAPE_2x4:    return dispatch<2, 4, 2, false>(k, io, s);
+    case CRAW_K_DN_SHAPE_2x8_X2: return dispatch<2, 8, 1, true>(k, io, s);
+    case CRAW_K_DN_SHAPE_2x4_X2: return dispatch<2, 4, 2, true>(k, io, s);
     default:                  return -22;
     }
 }

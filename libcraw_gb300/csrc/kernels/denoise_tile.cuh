@@ -75,7 +75,7 @@ CRAW_DEV void load_quad_f32(const float *base, size_t pitch, int qx, int qy, flo
     q[0] = a.x; q[1] = a.y; q[2] = b.x; q[3] = b.y;
 }
 
-template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY>
+template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2 = false>
 struct Cfg {
     static constexpr int R = SPATIAL ? S + P : 0;       /* apron of the tile */
     static constexpr int OX = 16 * BW, OY = 2 * M * WP;  /* plane samples per tile */
@@ -85,7 +85,10 @@ struct Cfg {
     static constexpr int EX = TX + 2, EY = TY + 2;       /* history: one more ring */
     static constexpr int EN = EX * EY;
     static constexpr int NT = 4 * WP * 32;
-    static constexpr int smem_floats = 4 * TN * (HISTORY ? 2 : 1) + (HISTORY ? 8 * EN : 0);
+    /* The packed search (X2, no history) keeps a copy of the tile shifted
+     * left by one sample, so that odd column pairs load as aligned float2. */
+    static constexpr bool PACKED = X2 && SPATIAL && !HISTORY;
+    static constexpr int smem_floats = 4 * TN * (HISTORY || PACKED ? 2 : 1) + (HISTORY ? 8 * EN : 0);
 };
 
 /* The NLM search of one thread: BW columns x M rows of one plane, at the
@@ -203,12 +206,147 @@ struct Search {
     }
 };
 
+/* Two fp32 lanes in one 64-bit register, for the sm_100 family's packed
+ * f32x2 add / sub / mul / fma (one instruction for both columns of a
+ * thread, the same IEEE rounding per lane as the scalar forms). */
+typedef unsigned long long f2x;
+
+CRAW_DEV f2x f2_pack(float lo, float hi)
+{
+    f2x r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+    return r;
+}
+CRAW_DEV float f2_lo(f2x a)
+{
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a));
+    return lo;
+}
+CRAW_DEV float f2_hi(f2x a)
+{
+    float lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a));
+    return hi;
+}
+CRAW_DEV f2x f2_add(f2x a, f2x b)
+{
+    f2x d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+CRAW_DEV f2x f2_sub(f2x a, f2x b)
+{
+    f2x d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+CRAW_DEV f2x f2_mul(f2x a, f2x b)
+{
+    f2x d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+CRAW_DEV f2x f2_fma(f2x a, f2x b, f2x c)
+{
+    f2x d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+CRAW_DEV f2x f2_ld(const float *p)   /* p 8-byte aligned */
+{
+    return *reinterpret_cast<const f2x *>(p);
+}
+
+/* The no-history search of a thread's 2 columns x M rows with the two
+ * columns in one packed register: squared differences, the column sums of
+ * the patch, the weight's affine step, the weight sum and the weighted
+ * sum are f32x2 instructions; the row sums (which mix the columns), the
+ * clamp and the exp2 stay scalar. `Tp` is the tile, `To` the same tile
+ * shifted left by one sample. Same arithmetic as Search (without fused
+ * multiply-adds in the squared differences). */
+template <int M, int R, int TS>
+struct SearchX2 {
+    static_assert(M % 2 == 0, "pairs of rows");
+    static_assert(R - 1 == S, "window origin");
+    f2x own[M + 2][2];            /* columns (0,1), (2,3) of the patch block */
+    f2x acc[M], wsum[M];
+    f2x c1, c0;
+
+    CRAW_DEV void init(const float *To, int ox0, int oy0, float inv_h2)
+    {
+        /* Patch block columns ox0 + S .. ox0 + S + 3: odd start, so they
+         * are aligned pairs of the shifted copy at ox0 + S - 1. */
+#pragma unroll
+        for (int r = 0; r < M + 2; r++) {
+            const float *row = To + (oy0 + R - 1 + r) * TS + ox0 + S - 1;
+            own[r][0] = f2_ld(row);
+            own[r][1] = f2_ld(row + 2);
+        }
+        const float kd = (1.0f / 9.0f) * inv_h2;
+        c1 = f2_pack(-kLog2e * kd, -kLog2e * kd);
+        c0 = f2_pack(2.0f * kLog2e, 2.0f * kLog2e);
+#pragma unroll
+        for (int m = 0; m < M; m++)
+            acc[m] = wsum[m] = f2_pack(0.0f, 0.0f);
+    }
+
+    CRAW_DEV void step_dy(const float *Tp, const float *To, int ox0, int oy0, int dy)
+    {
+        /* The shifted rows of this dy: columns ox0 .. ox0 + 9 as aligned
+         * pairs (even starts) and odd pairs (from the shifted copy). */
+        f2x ev[M + 2][5], od[M + 2][4];
+#pragma unroll
+        for (int r = 0; r < M + 2; r++) {
+            const int o = (oy0 + R - 1 + dy + r) * TS + ox0;
+#pragma unroll
+            for (int k = 0; k < 5; k++)
+                ev[r][k] = f2_ld(Tp + o + 2 * k);
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                od[r][k] = f2_ld(To + o + 2 * k);
+        }
+#pragma unroll
+        for (int o = 0; o <= 2 * S; o++) {
+            /* Patch-block columns c = 0..3 meet window columns c + o. */
+            f2x h[M + 2];
+#pragma unroll
+            for (int r = 0; r < M + 2; r++) {
+                const f2x w0 = (o & 1) ? od[r][o >> 1] : ev[r][o >> 1];
+                const f2x w1 = (o & 1) ? od[r][(o >> 1) + 1] : ev[r][(o >> 1) + 1];
+                const f2x d0 = f2_sub(own[r][0], w0), d1 = f2_sub(own[r][1], w1);
+                const f2x e0 = f2_mul(d0, d0), e1 = f2_mul(d1, d1);
+                /* Row sums of three, the middle pair shared. */
+                const float mid = f2_hi(e0) + f2_lo(e1);
+                h[r] = f2_pack(f2_lo(e0) + mid, mid + f2_hi(e1));
+            }
+#pragma unroll
+            for (int m = 0; m < M; m += 2) {
+                /* Column sums of three, the middle pair shared by two rows. */
+                const f2x mid = f2_add(h[m + 1], h[m + 2]);
+                const f2x d2a = f2_add(h[m], mid), d2b = f2_add(mid, h[m + 3]);
+                const f2x xa = f2_fma(d2a, c1, c0), xb = f2_fma(d2b, c1, c0);
+                const f2x wa = f2_pack(craw_ex2(fminf(f2_lo(xa), 0.0f)), craw_ex2(fminf(f2_hi(xa), 0.0f)));
+                const f2x wb = f2_pack(craw_ex2(fminf(f2_lo(xb), 0.0f)), craw_ex2(fminf(f2_hi(xb), 0.0f)));
+                /* The shifted centres: window columns 1 + o, 2 + o. */
+                const f2x qa = (o & 1) ? ev[m + 1][(o + 1) >> 1] : od[m + 1][o >> 1];
+                const f2x qb = (o & 1) ? ev[m + 2][(o + 1) >> 1] : od[m + 2][o >> 1];
+                wsum[m] = f2_add(wsum[m], wa);
+                wsum[m + 1] = f2_add(wsum[m + 1], wb);
+                acc[m] = f2_fma(wa, qa, acc[m]);
+                acc[m + 1] = f2_fma(wb, qb, acc[m + 1]);
+            }
+        }
+    }
+};
+
 /* One tile (tile column bx, tile row by) of all four planes; the whole
  * CTA takes part. `smem` holds Cfg::smem_floats floats. */
-template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY>
+template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2 = false>
 CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int bx, int by, float *smem)
 {
-    using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>;
+    using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2>;
+    static_assert(!C::PACKED || BW == 2, "the packed search pairs a thread's two columns");
     constexpr int R = C::R, OX = C::OX, OY = C::OY, TX = C::TX, TY = C::TY, TS = C::TS;
     constexpr int NT = C::NT;
     float *T = smem;                                 /* 4 planes of TN */
@@ -228,8 +366,13 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
             uint32_t q[4];
             load_quad_u16(io, qx, qy, q);
 #pragma unroll
-            for (int pl = 0; pl < 4; pl++)
-                T[pl * C::TN + r * TS + c] = gat_fwd(k, level(k, q[pl], pl));
+            for (int pl = 0; pl < 4; pl++) {
+                const float t = gat_fwd(k, level(k, q[pl], pl));
+                T[pl * C::TN + r * TS + c] = t;
+                if constexpr (C::PACKED)
+                    if (c > 0)
+                        T[(4 + pl) * C::TN + r * TS + c - 1] = t;
+            }
         }
     } else {
         for (int i = tid; i < C::EN; i += NT) {
@@ -283,7 +426,19 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
     const float *Tp = T + pl * C::TN;
     float res[M][BW];
 
-    if constexpr (SPATIAL) {
+    if constexpr (C::PACKED) {
+        const float *To = T + (4 + pl) * C::TN;
+        SearchX2<M, R, TS> st;
+        st.init(To, ox0, oy0, k.inv_h2);
+#pragma unroll 1
+        for (int dy = -S; dy <= S; dy++)
+            st.step_dy(Tp, To, ox0, oy0, dy);
+#pragma unroll
+        for (int m = 0; m < M; m++) {
+            res[m][0] = __fdiv_rn(f2_lo(st.acc[m]), f2_lo(st.wsum[m]));
+            res[m][1] = __fdiv_rn(f2_hi(st.acc[m]), f2_hi(st.wsum[m]));
+        }
+    } else if constexpr (SPATIAL) {
         const float *Vp = V + pl * C::TN;
         Search<BW, M, R, TS, HISTORY> st;
         st.init(Tp, Vp, ox0, oy0, k.inv_h2);

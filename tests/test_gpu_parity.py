@@ -108,6 +108,49 @@ def test_denoise_mosaic_vs_oracle(ctx):
         assert np.abs(got.astype(np.int32) - m.astype(np.int32)).mean() > 0.5
 
 
+@pytest.mark.parametrize("shape", range(len(L.DN_SHAPES)), ids=list(L.DN_SHAPES))
+@pytest.mark.parametrize("temporal", [False, True])
+def test_every_denoise_shape_vs_oracle(ctx, shape, temporal):
+    """Each denoise tile shape (the scalar and the packed f32x2 searches),
+    forced past the autotuner, on a ragged frame: the denoised mosaic within
+    one 16-bit code of the oracle's, over a three-frame temporal sequence
+    when `temporal` (the first frame has no history, the others have)."""
+    from gpu_util import download_image, upload_mosaic, alloc_rgba
+    w, h = 202, 134
+    prof = W.make_profile()
+    model = W.noise_model(8.0, 80.0)
+    flags = L.FLAG_DENOISE | L.FLAG_KEEP_INTERMEDIATE | (L.FLAG_TEMPORAL_DENOISE if temporal else 0)
+    kw = dict(denoise_strength=1.0, noise_override=model)
+    if temporal:
+        kw["denoise_temporal_strength"] = 0.8
+    fp = L.frame_params(prof, **kw)
+    frames = [W.synth_frame(w, h, 41, frame=i, rects=10, zone_plates=1, noise_a_dn=8.0,
+                            noise_b_dn=80.0, movers=[(2.0, 0.5), (8.0, 2.0)]) for i in range(3 if temporal else 1)]
+    L.debug_force_denoise_shape(shape)
+    try:
+        with L.Pipeline(ctx, L.pipeline_params(w, h, flags=flags, out_format=L.FORMAT_RGBA32F)) as pipe:
+            assert pipe.kernel_config() == (shape, shape)
+            prev = None
+            for m in frames:
+                _, src = upload_mosaic(m)
+                _, dst = alloc_rgba(w, h)
+                pipe.record(torch.cuda.current_stream().cuda_stream, src, dst, fp)
+                _, mos = pipe.intermediate()
+                got = download_image(mos, "r16")
+                ref, _ = orc.denoise_temporal(m, prof, model, 1.0, 0.8 if temporal else 0.0, prev)
+                d = np.abs(got.astype(np.int32) - ref.astype(np.int32))
+                limit = 2 if prev is not None else 1
+                assert d.max() <= limit, d.max()
+                assert (d > 0).mean() < 0.02, (d > 0).mean()
+                if temporal:
+                    # Follow the GPU's own state so the comparison does not drift.
+                    lvl, var = pipe.temporal_state()
+                    qv = (download_image(var, "r8").astype(np.float32) / 255.0) ** 2
+                    prev = np.stack([download_image(lvl, "r32f"), qv]).astype(np.float32)
+    finally:
+        L.debug_force_denoise_shape(-1)
+
+
 @pytest.mark.parametrize("storage", [L.STORAGE_FP32, L.STORAGE_FP16])
 @pytest.mark.parametrize("deb", [L.DEBAYER_BILINEAR, L.DEBAYER_RCD])
 @pytest.mark.parametrize("chroma", [False, True])
