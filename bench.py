@@ -47,6 +47,12 @@ METRIC = "5760x3240 frames/s full develop; p50/p99 frame latency at <=1e-3 rel e
 WORKLOAD = "5760x3240 RGGB 12-bit: VST + NLM 1.0 + RCD + ACES AP1 (RGC) float32 + AWB histogram"
 #: Denoise tile shapes by craw_pipeline_get_kernel_config() index.
 DN_SHAPES = ["2x8", "2x4", "2x8 f32x2", "2x4 f32x2"]
+#: dram__bytes_read.sum + dram__bytes_write.sum of one launch of the stage's
+#: kernel at 5760x3240 (ncu captures summarised in profiles/denoise_nlm_5760x3240.md).
+DRAM_BYTES_5760x3240 = {
+    ("denoise_nlm", "2x8 f32x2"): 37.365e6 + 1.070e6,
+    ("denoise_nlm", "2x8"): 37.37e6 + 0.66e6,
+}
 
 
 def parse():
@@ -59,6 +65,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the plain/fp16/cpu side runs")
     ap.add_argument("--extras", default="plain,fp16,batch,temporal,serve,cpu",
                     help="comma list of side runs: plain, fp16, batch, temporal, serve, cpu")
+    ap.add_argument("--force-shape", type=int, default=-1,
+                    help="denoise tile shape index instead of the autotuner's (profiling)")
     ap.add_argument("--width", type=int, default=5760)
     ap.add_argument("--height", type=int, default=3240)
     return ap.parse_args()
@@ -268,6 +276,9 @@ def run_gpu(args):
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     ctx = L.Context(dev)
+    if args.force_shape >= 0:
+        # A fixed denoise shape and no autotuner launches, for profiling runs.
+        L.debug_force_denoise_shape(args.force_shape)
     stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
 
@@ -325,8 +336,13 @@ def run_gpu(args):
         bpp = {"denoise_nlm": 4.0, "develop": 18.0 + 8.0 / 64, "plain_denoise": 4.0,
                "plain_develop": 18.0}.get(dom, 4.0)
         achieved = bpp * n_px / (dom_ms / 1000.0) / 1e9
+        # DRAM bytes (read + write) of one launch from an ncu capture at
+        # 5760x3240 (profiles/), scaled by the pixels of this run.
+        traffic = DRAM_BYTES_5760x3240.get((dom, DN_SHAPES[kcfg[0]]))
+        if traffic is not None:
+            traffic = traffic * n_px / (5760 * 3240)
         roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"],
-                "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": None,
+                "unit": "GB/s", "frac": achieved / pk["hbm_gbs"], "traffic": traffic,
                 "peak_src": pk["src"], "bytes_per_px": bpp, "ms_per_launch": dom_ms}
         if dom.endswith("denoise_nlm") or dom == "plain_denoise":
             clk_s = clk.summary()
@@ -402,6 +418,10 @@ def run_gpu(args):
             extras["speedup_vs_plain_fp32"] = (args.steps / total_s) / base
         if "batch" in want:
             extras["batch"] = run_batch_mix(ctx, stream, max(5, args.steps // 3), 3)
+            small = [W.BatchFrame(640, 360, 41000 + i, 4.0, 40.0) for i in range(64)]
+            extras["batch_small"] = run_batch_mix(
+                ctx, stream, max(5, args.steps // 3), 3, small,
+                "64 frames of 640x360 (previews), NLM 1.0 + RCD + BT.2020 float32")
             if base:
                 extras["batch"]["eq_speedup_vs_plain_fp32"] = (
                     extras["batch"]["fused_graph"]["eq_5760x3240_fps"] / base)
@@ -453,17 +473,18 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
-def run_batch_mix(ctx, stream, steps: int, warmup: int) -> dict:
+def run_batch_mix(ctx, stream, steps: int, warmup: int, mix=None, label: str | None = None) -> dict:
     """The batched workload (16 frames of four sizes, NLM 1.0 + RCD + BT.2020
     float32) as one recording of the batch API: a persistent fused launch
     replayed from a captured CUDA graph; beside it the unfused and
     graph-less variants and the same 16 frames through the single-frame
-    pipeline one after another. Inputs (336 MB) are larger than L2."""
+    pipeline one after another. Inputs (336 MB) are larger than L2.
+    `mix` / `label` run another list of frames the same way."""
     import torch
     import libcraw_gb300 as L
     from libcraw_gb300 import workloads as W
 
-    mix = W.batch_mix()
+    mix = mix or W.batch_mix()
     prof = W.make_profile()
     mw, mh = max(f.width for f in mix), max(f.height for f in mix)
     srcs, dsts, fps, keep = [], [], [], []
@@ -496,8 +517,8 @@ def run_batch_mix(ctx, stream, steps: int, warmup: int) -> dict:
                 "mpx_per_s": n_px / 1e3 / statistics.mean(ms),
                 "eq_5760x3240_fps": n_px / (5760 * 3240) * 1000.0 / statistics.mean(ms)}
 
-    res = {"workload": "16 frames: 6x1920x1080, 4x3840x2160, 4x5760x3240, 2x6000x4000; "
-                       "NLM 1.0 + RCD + BT.2020 float32; noise a~U[1,8], b~U[10,80] per frame",
+    res = {"workload": label or ("16 frames: 6x1920x1080, 4x3840x2160, 4x5760x3240, 2x6000x4000; "
+                                 "NLM 1.0 + RCD + BT.2020 float32; noise a~U[1,8], b~U[10,80] per frame"),
            "mpx": n_px / 1e6}
     for name, flags in (("fused_graph", 0), ("unfused_graph", L.BATCH_FLAG_UNFUSED),
                         ("fused_no_graph", L.BATCH_FLAG_NO_GRAPH)):

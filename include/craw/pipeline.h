@@ -245,8 +245,7 @@ CRAW_API int craw_pipeline_get_temporal_state(CRAWPipeline *pipe, CRAWImage *lev
 /* Extension, no counterpart in the reference: the tile shapes the
  * autotuner chose for the denoise kernel, without and with a temporal
  * history (0: 2 columns x 8 rows a thread, 1: 2 x 4; 2 and 3: the same
- * with the search in packed f32x2 arithmetic, which has no history form,
- * so with a history they run the scalar search). */
+ * with the search in packed f32x2 arithmetic). */
 CRAW_API int craw_pipeline_get_kernel_config(CRAWPipeline *pipe, int *denoise_shape,
                                              int *denoise_shape_history);
 

@@ -46,8 +46,8 @@ typedef struct CRAWKDenoiseIO {
 enum CRAWKDenoiseShape {
     CRAW_K_DN_SHAPE_2x8 = 0,     /* a thread filters 2 columns x 8 rows */
     CRAW_K_DN_SHAPE_2x4,         /* 2 columns x 4 rows */
-    CRAW_K_DN_SHAPE_2x8_X2,      /* 2x8 with the packed f32x2 search (no history) */
-    CRAW_K_DN_SHAPE_2x4_X2,      /* 2x4 with the packed f32x2 search (no history) */
+    CRAW_K_DN_SHAPE_2x8_X2,      /* 2x8 with the search in packed f32x2 arithmetic */
+    CRAW_K_DN_SHAPE_2x4_X2,      /* 2x4 with the search in packed f32x2 arithmetic */
     CRAW_K_DN_SHAPE_NB,
 };
 
@@ -156,8 +156,8 @@ typedef struct CRAWKBatchFrame {
 
 /* Denoise tile shapes of the batch kernel (256 threads). */
 enum CRAWKBatchShape {
-    CRAW_K_BATCH_DN_2x4 = 0,    /* 2 columns x 4 rows a thread, 32x16 tiles */
-    CRAW_K_BATCH_DN_2x8,        /* 2 x 8, 32x32 tiles */
+    CRAW_K_BATCH_DN_2x4 = 0,    /* 2 columns x 4 rows a thread, 32x16 tiles, packed f32x2 */
+    CRAW_K_BATCH_DN_2x8,        /* 2 x 8, 32x32 tiles, packed f32x2 */
     CRAW_K_BATCH_DN_NB,
 };
 

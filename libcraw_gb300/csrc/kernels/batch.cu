@@ -27,8 +27,10 @@ using namespace craw_dev;
 
 constexpr int NT = 256;
 
+/* The denoise of a batch: the packed f32x2 search, 2 columns x M rows a
+ * thread, 256 threads. */
 template <int M> struct DnShape {
-    using C = craw_dn::Cfg<2, M, 2, true, false, false>;
+    using C = craw_dn::Cfg<2, M, 2, true, false, false, true>;
 };
 
 /* The frame an item of a phase belongs to: the last one whose first item
@@ -49,7 +51,7 @@ CRAW_DEV void denoise_phase(const CRAWKBatchTable &T, int nb, int items, float *
         const CRAWKBatchFrame &F = T.f[item_frame(T, nb, it, false)];
         const int local = it - F.dn_first;
         __syncthreads();   /* the previous item's shared memory is free */
-        craw_dn::denoise_tile<2, M, 2, true, false, false>(F.dn, F.dio, local % F.dn_tx,
+        craw_dn::denoise_tile<2, M, 2, true, false, false, true>(F.dn, F.dio, local % F.dn_tx,
                                                            local / F.dn_tx, smem);
     }
 }

@@ -36,8 +36,7 @@ int launch(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, cudaStream_t s)
     return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }
 
-/* X2: the packed search where there is no history; with a history the
- * shape runs the scalar search (the packed one has no history form). */
+/* X2: the search in packed f32x2 arithmetic. */
 template <int BW, int M, int WP, bool X2>
 int dispatch(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, cudaStream_t s)
 {
@@ -45,7 +44,7 @@ int dispatch(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, cudaStream_t s)
     const bool hi = te && (k->mode & CRAW_K_DN_HISTORY);
     if (sp && !te)  return launch<BW, M, WP, true, false, false, X2>(k, io, s);
     if (sp && !hi)  return launch<BW, M, WP, true, true, false, X2>(k, io, s);
-    if (sp)         return launch<BW, M, WP, true, true, true, false>(k, io, s);
+    if (sp)         return launch<BW, M, WP, true, true, true, X2>(k, io, s);
     if (te && !hi)  return launch<BW, M, WP, false, true, false, false>(k, io, s);
     if (te)         return launch<BW, M, WP, false, true, true, false>(k, io, s);
     return -22;

@@ -85,10 +85,14 @@ struct Cfg {
     static constexpr int EX = TX + 2, EY = TY + 2;       /* history: one more ring */
     static constexpr int EN = EX * EY;
     static constexpr int NT = 4 * WP * 32;
-    /* The packed search (X2, no history) keeps a copy of the tile shifted
-     * left by one sample, so that odd column pairs load as aligned float2. */
-    static constexpr bool PACKED = X2 && SPATIAL && !HISTORY;
-    static constexpr int smem_floats = 4 * TN * (HISTORY || PACKED ? 2 : 1) + (HISTORY ? 8 * EN : 0);
+    /* The packed search (X2) keeps copies of the tile (and, with a
+     * history, of the variance) shifted left by one sample, so that odd
+     * column pairs load as aligned float2: TO and VO, after the rest. */
+    static constexpr bool PACKED = X2 && SPATIAL;
+    static constexpr int TO_OFF = HISTORY ? 8 * TN + 8 * EN : 4 * TN;
+    static constexpr int VO_OFF = TO_OFF + 4 * TN;
+    static constexpr int smem_floats = 4 * TN * (HISTORY ? 2 : 1) + (HISTORY ? 8 * EN : 0) +
+                                       (PACKED ? 4 * TN * (HISTORY ? 2 : 1) : 0);
 };
 
 /* The NLM search of one thread: BW columns x M rows of one plane, at the
@@ -258,22 +262,24 @@ CRAW_DEV f2x f2_ld(const float *p)   /* p 8-byte aligned */
     return *reinterpret_cast<const f2x *>(p);
 }
 
-/* The no-history search of a thread's 2 columns x M rows with the two
- * columns in one packed register: squared differences, the column sums of
- * the patch, the weight's affine step, the weight sum and the weighted
- * sum are f32x2 instructions; the row sums (which mix the columns), the
- * clamp and the exp2 stay scalar. `Tp` is the tile, `To` the same tile
- * shifted left by one sample. Same arithmetic as Search (without fused
- * multiply-adds in the squared differences). */
-template <int M, int R, int TS>
+/* The search of a thread's 2 columns x M rows with the two columns in one
+ * packed register: squared differences, the column sums of the patch, the
+ * weight's affine steps, the weight sum and the weighted sum are f32x2
+ * instructions; the row sums (which mix the columns), the clamp and the
+ * exp2 stay scalar. `Tp` is the tile, `To` the same tile shifted left by
+ * one sample; with a history `Vp` / `Vo` are the variance and its shifted
+ * copy. Same arithmetic as Search (without fused multiply-adds in the
+ * squared differences). */
+template <int M, int R, int TS, bool HISTORY>
 struct SearchX2 {
     static_assert(M % 2 == 0, "pairs of rows");
     static_assert(R - 1 == S, "window origin");
     f2x own[M + 2][2];            /* columns (0,1), (2,3) of the patch block */
     f2x acc[M], wsum[M];
-    f2x c1, c0;
+    f2x vc[HISTORY ? M : 1], lvc[HISTORY ? M : 1];
+    f2x c1, c0, nkd;
 
-    CRAW_DEV void init(const float *To, int ox0, int oy0, float inv_h2)
+    CRAW_DEV void init(const float *To, const float *Vp, int ox0, int oy0, float inv_h2)
     {
         /* Patch block columns ox0 + S .. ox0 + S + 3: odd start, so they
          * are aligned pairs of the shifted copy at ox0 + S - 1. */
@@ -286,12 +292,20 @@ struct SearchX2 {
         const float kd = (1.0f / 9.0f) * inv_h2;
         c1 = f2_pack(-kLog2e * kd, -kLog2e * kd);
         c0 = f2_pack(2.0f * kLog2e, 2.0f * kLog2e);
+        nkd = f2_pack(-kd, -kd);
 #pragma unroll
-        for (int m = 0; m < M; m++)
+        for (int m = 0; m < M; m++) {
             acc[m] = wsum[m] = f2_pack(0.0f, 0.0f);
+            if constexpr (HISTORY) {
+                /* The centres' variance: columns ox0 + R, + R + 1 (aligned). */
+                vc[m] = f2_ld(Vp + (oy0 + R + m) * TS + ox0 + R);
+                lvc[m] = f2_pack(__fdiv_rn(kLog2e, f2_lo(vc[m])), __fdiv_rn(kLog2e, f2_hi(vc[m])));
+            }
+        }
     }
 
-    CRAW_DEV void step_dy(const float *Tp, const float *To, int ox0, int oy0, int dy)
+    CRAW_DEV void step_dy(const float *Tp, const float *To, const float *Vp, const float *Vo,
+                          int ox0, int oy0, int dy)
     {
         /* The shifted rows of this dy: columns ox0 .. ox0 + 9 as aligned
          * pairs (even starts) and odd pairs (from the shifted copy). */
@@ -325,7 +339,19 @@ struct SearchX2 {
                 /* Column sums of three, the middle pair shared by two rows. */
                 const f2x mid = f2_add(h[m + 1], h[m + 2]);
                 const f2x d2a = f2_add(h[m], mid), d2b = f2_add(mid, h[m + 3]);
-                const f2x xa = f2_fma(d2a, c1, c0), xb = f2_fma(d2b, c1, c0);
+                f2x xa, xb;
+                if constexpr (HISTORY) {
+                    /* The shifted centres' variance, window columns 1 + o, 2 + o. */
+                    const int vcol = (o & 1) ? ox0 + 1 + o : ox0 + o;
+                    const float *vsrc = (o & 1) ? Vp : Vo;
+                    const f2x vqa = f2_ld(vsrc + (oy0 + R + dy + m) * TS + vcol);
+                    const f2x vqb = f2_ld(vsrc + (oy0 + R + dy + m + 1) * TS + vcol);
+                    xa = f2_mul(f2_fma(d2a, nkd, f2_add(vc[m], vqa)), lvc[m]);
+                    xb = f2_mul(f2_fma(d2b, nkd, f2_add(vc[m + 1], vqb)), lvc[m + 1]);
+                } else {
+                    xa = f2_fma(d2a, c1, c0);
+                    xb = f2_fma(d2b, c1, c0);
+                }
                 const f2x wa = f2_pack(craw_ex2(fminf(f2_lo(xa), 0.0f)), craw_ex2(fminf(f2_hi(xa), 0.0f)));
                 const f2x wb = f2_pack(craw_ex2(fminf(f2_lo(xb), 0.0f)), craw_ex2(fminf(f2_hi(xb), 0.0f)));
                 /* The shifted centres: window columns 1 + o, 2 + o. */
@@ -371,7 +397,7 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
                 T[pl * C::TN + r * TS + c] = t;
                 if constexpr (C::PACKED)
                     if (c > 0)
-                        T[(4 + pl) * C::TN + r * TS + c - 1] = t;
+                        smem[C::TO_OFF + pl * C::TN + r * TS + c - 1] = t;
             }
         }
     } else {
@@ -412,8 +438,14 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
                 float a = k.t_alpha * expf(-fmaxf(x, 0.0f));
                 float sp = (float)sv[pl] * (1.0f / 255.0f);
                 float vv = __fadd_rn(__fmul_rn(1.0f - a, 1.0f - a), __fmul_rn(a * a, sp * sp));
-                T[pl * C::TN + r * TS + c] = __fadd_rn(__fmul_rn(cp[e0], 1.0f - a), __fmul_rn(pp[e0], a));
+                const float t = __fadd_rn(__fmul_rn(cp[e0], 1.0f - a), __fmul_rn(pp[e0], a));
+                T[pl * C::TN + r * TS + c] = t;
                 V[pl * C::TN + r * TS + c] = fmaxf(vv, kVarMin);
+                if constexpr (C::PACKED)
+                    if (c > 0) {
+                        smem[C::TO_OFF + pl * C::TN + r * TS + c - 1] = t;
+                        smem[C::VO_OFF + pl * C::TN + r * TS + c - 1] = fmaxf(vv, kVarMin);
+                    }
             }
         }
     }
@@ -427,12 +459,13 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
     float res[M][BW];
 
     if constexpr (C::PACKED) {
-        const float *To = T + (4 + pl) * C::TN;
-        SearchX2<M, R, TS> st;
-        st.init(To, ox0, oy0, k.inv_h2);
+        const float *To = smem + C::TO_OFF + pl * C::TN;
+        const float *Vp = V + pl * C::TN, *Vo = smem + C::VO_OFF + pl * C::TN;
+        SearchX2<M, R, TS, HISTORY> st;
+        st.init(To, Vp, ox0, oy0, k.inv_h2);
 #pragma unroll 1
         for (int dy = -S; dy <= S; dy++)
-            st.step_dy(Tp, To, ox0, oy0, dy);
+            st.step_dy(Tp, To, Vp, Vo, ox0, oy0, dy);
 #pragma unroll
         for (int m = 0; m < M; m++) {
             res[m][0] = __fdiv_rn(f2_lo(st.acc[m]), f2_lo(st.wsum[m]));
