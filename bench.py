@@ -139,15 +139,22 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "src": "fallback"}
 
 
-def dist_init():
+def dist_init(backend: str = "nccl"):
+    """Rank, world size and local rank from the torchrun environment; joins
+    the process group (NCCL on the GPUs; gloo for the CPU tests of this
+    logic). Replicas: no collective touches the data path, only a barrier
+    around the timed region and the max of the timings."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
         return 0, 1, 0
     import torch.distributed as dist
     rank, local = int(os.environ["RANK"]), int(os.environ.get("LOCAL_RANK", "0"))
     import torch
-    torch.cuda.set_device(local)
-    dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    if backend == "nccl":
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    else:
+        dist.init_process_group(backend)
     return rank, ws, local
 
 
@@ -162,9 +169,22 @@ def max_over_ranks(x: float, ws: int) -> float:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def replica_seed(base: int, rank: int, i: int) -> int:
+    """Seed of frame `i` of a rank: every replica develops frames of its own."""
+    return base + 7919 * rank + i
+
+
+def whole_job_rate(units_per_rank: int, ws: int, seconds_per_rank: float) -> float:
+    """Units all ranks processed over the slowest rank's time (weak scaling:
+    per-rank work is fixed, so the job is as fast as its slowest rank)."""
+    slowest = max_over_ranks(seconds_per_rank, ws)
+    return ws * units_per_rank / slowest
 
 
 # ------------------------------------------------------------- CPU baseline
@@ -267,7 +287,7 @@ def run_gpu(args):
 
     # Four distinct frames in rotation (different seeds), 16-byte rows.
     nfr = 4
-    host_frames = [W.synth_frame(w, h, c.seed + 7919 * rank + i, rects=c.rects, zone_plates=c.zone_plates,
+    host_frames = [W.synth_frame(w, h, replica_seed(c.seed, rank, i), rects=c.rects, zone_plates=c.zone_plates,
                                  noise_a_dn=c.noise_a_dn, noise_b_dn=c.noise_b_dn) for i in range(nfr)]
     dev_frames = [torch.from_numpy(f.view(np.int16)).cuda() for f in host_frames]
     srcs = [L.Image(t.data_ptr(), w * 2, L.FORMAT_R16_UNORM, w, h) for t in dev_frames]
@@ -318,8 +338,7 @@ def run_gpu(args):
     with ClockSampler(dev) as clk:
         ms, stage, wall = timed(pipe, args.steps, max(3, args.warmup))
     total_s = sum(ms) / 1000.0
-    slowest = max_over_ranks(total_s, ws)
-    value = ws * args.steps / slowest
+    value = whole_job_rate(args.steps, ws, total_s)
     lat = sorted(ms)
     hist = pipe.awb_histogram()
 

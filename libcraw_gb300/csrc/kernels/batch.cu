@@ -26,6 +26,7 @@ namespace cg = cooperative_groups;
 using namespace craw_dev;
 
 constexpr int NT = 256;
+constexpr int BQH = 16;     /* rows of a develop item (a 64 x 16 quad tile) */
 
 /* The denoise of a batch: the packed f32x2 search, 2 columns x M rows a
  * thread, 256 threads. */
@@ -62,27 +63,27 @@ CRAW_DEV void develop_phase(const CRAWKBatchTable &T, int nb, int items, float *
     for (int it = blockIdx.x; it < items; it += gridDim.x) {
         const CRAWKBatchFrame &F = T.f[item_frame(T, nb, it, true)];
         const int local = it - F.dv_first;
-        const int x0 = (local % F.dv_tx) * QTW, y0 = (local / F.dv_tx) * QTH;
+        const int x0 = (local % F.dv_tx) * QTW, y0 = (local / F.dv_tx) * BQH;
         __syncthreads();
         if constexpr (METHOD == kRcd) {
-            if (quad_interior(x0, y0, F.dv.width, F.dv.height)) {
-                rcd_quad_tile(F.dv, F.vio, x0, y0, smem);
+            if (quad_interior<BQH>(x0, y0, F.dv.width, F.dv.height)) {
+                rcd_quad_tile<BQH, NT>(F.dv, F.vio, x0, y0, smem);
                 continue;
             }
         }
-        /* Per-pixel tiles of BTW x BTH cover the QTW x QTH item. */
+        /* Per-pixel tiles of BTW x BTH cover the QTW x BQH item. */
         for (int sx = 0; sx < QTW; sx += BTW) {
             if (x0 + sx >= F.dv.width)
                 break;
             __syncthreads();
-            pixel_tile<METHOD, BTW, BTH, NT>(F.dv, F.vio, x0 + sx, y0, smem);
+            pixel_tile<METHOD, BTW, BTH, NT, BQH>(F.dv, F.vio, x0 + sx, y0, smem);
         }
     }
 }
 
 template <int M, int METHOD> struct Smem {
     static constexpr int dn = DnShape<M>::C::smem_floats;
-    static constexpr int dv = METHOD == kRcd ? RcdQuads<QTW, QTH, NT>::floats : 0;
+    static constexpr int dv = METHOD == kRcd ? RcdQuads<QTW, BQH, NT>::floats : 0;
     static constexpr int px = PixelSmem<METHOD, BTW, BTH, NT>::floats;
     static constexpr int a = dn > dv ? dn : dv;
     static constexpr int floats = a > px ? a : px;
@@ -170,7 +171,7 @@ int run(const CRAWKBatchTable *T, int nb, int dn_items, int dv_items, int fused,
     }
     {
         auto k = k_batch_develop<METHOD>;
-        const size_t sm = (METHOD == kRcd ? RcdQuads<QTW, QTH, NT>::floats
+        const size_t sm = (METHOD == kRcd ? RcdQuads<QTW, BQH, NT>::floats
                                           : PixelSmem<METHOD, BTW, BTH, NT>::floats) * sizeof(float);
         if (set_smem(k, sm) < 0)
             return -5;
@@ -204,7 +205,7 @@ extern "C" void craw_k_batch_tiles(int32_t w, int32_t h, int shape, int32_t *dn_
     *dn_tx = (w / 2 + ox - 1) / ox;
     *dn_ty = (h / 2 + oy - 1) / oy;
     *dv_tx = (w + QTW - 1) / QTW;
-    *dv_ty = (h + QTH - 1) / QTH;
+    *dv_ty = (h + BQH - 1) / BQH;
 }
 
 extern "C" int craw_k_batch(const CRAWKBatchTable *table, int32_t nb, int32_t dn_items,

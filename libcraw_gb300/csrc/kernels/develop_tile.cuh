@@ -591,34 +591,38 @@ template <int METHOD, int TW, int TH, int NT> struct PixelSmem {
     static constexpr int floats = work + 3 * TW * TH;
 };
 
-/* Interior tiles of the RCD by quads (QTW x QTH pixels, all aprons inside
- * the frame); the per-pixel kernel below takes the rest. */
+/* Interior tiles of the RCD by quads (QTW x QH pixels, all aprons inside
+ * the frame); the per-pixel kernel below takes the rest. The single-frame
+ * kernel uses QTH-row tiles with one thread per quad (QNT threads); the
+ * batch kernel its own height and thread count. */
 constexpr int QTW = 64, QTH = 16, QNT = 256, BTW = 32, BTH = 16;
 
+template <int QH = QTH>
 CRAW_DEV bool quad_interior(int x0, int y0, int w, int h)
 {
-    return x0 >= 6 && y0 >= 6 && x0 + QTW + 6 <= w && y0 + QTH + 6 <= h;
+    return x0 >= 6 && y0 >= 6 && x0 + QTW + 6 <= w && y0 + QH + 6 <= h;
 }
 
-/* One interior RCD tile at (x0, y0) by quads; QNT threads, `smem` holds
- * RcdQuads<QTW, QTH, QNT>::floats floats. */
+/* One interior RCD tile at (x0, y0) by quads; NQ threads, `smem` holds
+ * RcdQuads<QTW, QH, NQ>::floats floats. */
+template <int QH = QTH, int NQ = QNT>
 CRAW_DEV void rcd_quad_tile(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, int y0,
                             float *smem)
 {
-    RcdQuads<QTW, QTH, QNT> t;
+    RcdQuads<QTW, QH, NQ> t;
     t.carve(smem);
     t.load(k, io, x0, y0);
     __syncthreads();
     t.run();
-    epilogue<QTW, QTH, QNT>(k, io, x0, y0, t.rgb);
+    epilogue<QTW, QH, NQ>(k, io, x0, y0, t.rgb);
 }
 
 /* Per-pixel tiles: every bilinear and MHC tile, and the RCD tiles that the
  * quad kernel leaves (those whose QTW x QTH tile touches a border). */
 /* One per-pixel tile at (x0, y0); NT threads, `smem` holds
- * PixelSmem<METHOD, TW, TH, NT>::floats floats. An RCD tile inside a quad
- * tile that rcd_quad_tile() takes is skipped. */
-template <int METHOD, int TW, int TH, int NT>
+ * PixelSmem<METHOD, TW, TH, NT>::floats floats. An RCD tile inside a
+ * QTW x QH quad tile that rcd_quad_tile<QH>() takes is skipped. */
+template <int METHOD, int TW, int TH, int NT, int QH = QTH>
 CRAW_DEV void pixel_tile(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, int y0,
                          float *smem)
 {
@@ -636,8 +640,8 @@ CRAW_DEV void pixel_tile(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0
     f.interior = f.x0 >= A && f.y0 >= A && f.x0 + TW + A <= k.width && f.y0 + TH + A <= k.height;
 
     if constexpr (METHOD == kRcd) {
-        static_assert(QTW % TW == 0 && QTH == TH, "a quad tile is whole per-pixel tiles");
-        if (quad_interior(f.x0 / QTW * QTW, f.y0, k.width, k.height))
+        static_assert(QTW % TW == 0 && QH % TH == 0, "a quad tile is whole per-pixel tiles");
+        if (quad_interior<QH>(f.x0 / QTW * QTW, f.y0 / QH * QH, k.width, k.height))
             return;
         RcdTile<TW, TH, NT> t;
         t.carve(smem);
