@@ -120,10 +120,13 @@ CRAW_DEV void craw_load_rgb(const void *base, size_t pitch, int x, int y, int ha
  * blocks, divide the gains back out, bin ln(R/G), ln(B/G) over
  * [-2.5, 1] in 128 bins, weights min(g, 0.5) and g^4 in 16.16.
  *
- * The logarithm is taken in double and rounded once, which is the
- * correctly rounded float log; a block whose bin position lies within
- * 2e-4 of a bin edge, where a host logf an ulp away could choose the
- * other bin, is deferred to the host instead. */
+ * The logarithm is CUDA's logf (within 1 ulp, as the host's is): the two
+ * can differ by 2 ulp of ln(R/G), i.e. at most 2e-5 of a bin, so a block
+ * whose bin position lies within 2e-4 of a bin edge, where the two could
+ * choose different bins, is deferred to the host instead; every other
+ * block lands in the host's bin. (GB300's FP64 rate is a small fraction
+ * of its FP32 rate, so a double-precision log would cost more than the
+ * whole block sum.) */
 CRAW_DEV uint64_t craw_awb_block(float r, float g, float b, const float wb[3],
                                  CRAWKAwbDeferred *deferred, uint32_t *nb_deferred)
 {
@@ -132,7 +135,7 @@ CRAW_DEV uint64_t craw_awb_block(float r, float g, float b, const float wb[3],
         return 0;
     float rr = __fdiv_rn(__fdiv_rn(r, wb[0]), g);
     float bb = __fdiv_rn(__fdiv_rn(b, wb[2]), g);
-    float x = (float)log((double)rr), y = (float)log((double)bb);
+    float x = logf(rr), y = logf(bb);
     x = x > lmin ? (x < lmax ? x : lmax) : lmin;
     y = y > lmin ? (y < lmax ? y : lmax) : lmin;
     float fx = __fmul_rn(__fdiv_rn(__fsub_rn(x, lmin), span), 128.0f);

@@ -22,8 +22,10 @@ k_develop_rcd_quads(const CRAWKDevelop k, const CRAWKDevelopIO io)
     rcd_quad_tile(k, io, x0, y0, smem);
 }
 
+/* Eight CTAs an SM (full occupancy at 256 threads): the bilinear and MHC
+ * tiles are bound by HBM and need every warp in flight. */
 template <int METHOD, int TW, int TH, int NT>
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, 2048 / NT)
 k_develop(const CRAWKDevelop k, const CRAWKDevelopIO io)
 {
     extern __shared__ __align__(16) float smem[];

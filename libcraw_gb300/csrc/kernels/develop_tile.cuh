@@ -506,6 +506,7 @@ template <int TW, int TH, int NT>
 CRAW_DEV void epilogue(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, int y0, float *rgb)
 {
     constexpr int P = TW * TH;
+    static_assert(P % 4 == 0 && TW % 8 == 0, "planes and block rows are whole float4s");
     const bool chroma = io.quarter != nullptr;
     for (int i = threadIdx.x; i < P; i += NT) {
         int x = x0 + i % TW, y = y0 + i / TW;
@@ -568,13 +569,38 @@ CRAW_DEV void epilogue(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, 
             continue;
         int xe = min(8, k.width - (x0 + bx * 8)), ye = min(8, k.height - (y0 + by * 8));
         float s0 = 0.f, s1 = 0.f, s2 = 0.f;
-        for (int jj = 0; jj < ye; jj++)
-            for (int ii = 0; ii < xe; ii++) {
-                int j = (by * 8 + jj) * TW + bx * 8 + ii;
-                s0 = __fadd_rn(s0, rgb[j]);
-                s1 = __fadd_rn(s1, rgb[P + j]);
-                s2 = __fadd_rn(s2, rgb[2 * P + j]);
+        if (xe == 8 && ye == 8) {
+            /* A whole block: the same order, every row read as two 16-byte
+             * loads a channel ahead of its dependent adds (rows one at a
+             * time, so that the registers stay those of the rest). */
+#pragma unroll 1
+            for (int jj = 0; jj < 8; jj++) {
+                const int j = (by * 8 + jj) * TW + bx * 8;
+                const float4 r0 = *reinterpret_cast<const float4 *>(rgb + j);
+                const float4 r1 = *reinterpret_cast<const float4 *>(rgb + j + 4);
+                const float4 g0 = *reinterpret_cast<const float4 *>(rgb + P + j);
+                const float4 g1 = *reinterpret_cast<const float4 *>(rgb + P + j + 4);
+                const float4 b0 = *reinterpret_cast<const float4 *>(rgb + 2 * P + j);
+                const float4 b1 = *reinterpret_cast<const float4 *>(rgb + 2 * P + j + 4);
+                const float rr[8] = { r0.x, r0.y, r0.z, r0.w, r1.x, r1.y, r1.z, r1.w };
+                const float gg[8] = { g0.x, g0.y, g0.z, g0.w, g1.x, g1.y, g1.z, g1.w };
+                const float bb[8] = { b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w };
+#pragma unroll
+                for (int ii = 0; ii < 8; ii++) {
+                    s0 = __fadd_rn(s0, rr[ii]);
+                    s1 = __fadd_rn(s1, gg[ii]);
+                    s2 = __fadd_rn(s2, bb[ii]);
+                }
             }
+        } else {
+            for (int jj = 0; jj < ye; jj++)
+                for (int ii = 0; ii < xe; ii++) {
+                    int j = (by * 8 + jj) * TW + bx * 8 + ii;
+                    s0 = __fadd_rn(s0, rgb[j]);
+                    s1 = __fadd_rn(s1, rgb[P + j]);
+                    s2 = __fadd_rn(s2, rgb[2 * P + j]);
+                }
+        }
         float n = (float)(xe * ye);
         io.awb.rec[(size_t)(y0 / 8 + by) * blocks_x + x0 / 8 + bx] =
             craw_awb_block(__fdiv_rn(s0, n), __fdiv_rn(s1, n), __fdiv_rn(s2, n), k.awb_wb,
@@ -586,8 +612,9 @@ CRAW_DEV void epilogue(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, 
 
 template <int METHOD, int TW, int TH, int NT> struct PixelSmem {
     static constexpr int A = Apron<METHOD>::v;
-    static constexpr int work = METHOD == kRcd ? RcdTile<TW, TH, NT>::floats
-                                               : Tile<TW, TH, A, float>::N;
+    /* Rounded to 4 floats: the planar output after it is read as float4. */
+    static constexpr int work = ((METHOD == kRcd ? RcdTile<TW, TH, NT>::floats
+                                                 : Tile<TW, TH, A, float>::N) + 3) & ~3;
     static constexpr int floats = work + 3 * TW * TH;
 };
 
