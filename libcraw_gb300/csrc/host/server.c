@@ -37,6 +37,7 @@ struct job {
     CRAWFrameParams fp;
     double pts;
     uint64_t user;
+    uint64_t seq;                    /* submission order within the server */
     double t_submit, t_launch;
 };
 
@@ -303,7 +304,20 @@ static void awb_update(struct stream *st, struct job *j, CRAWServerResult *r)
     }
 }
 
-/* Retires every finished frame (lock held; dropped around AWB work). */
+/* The slot of a stream's oldest frame in flight, or NULL. */
+static struct slot *oldest_slot(struct stream *st)
+{
+    struct slot *o = NULL;
+    for (uint32_t k = 0; k < st->nb_slots; k++)
+        if (st->slots[k].job && (!o || st->slots[k].job->seq < o->job->seq))
+            o = &st->slots[k];
+    return o;
+}
+
+/* Retires every finished frame (lock held; dropped around AWB work). A
+ * stream's frames finish in submission order on its CUDA stream and are
+ * retired in that order: the oldest first, and none after one that is
+ * still running. */
 static bool retire_done(CRAWServer *s)
 {
     bool progress = false;
@@ -312,18 +326,18 @@ static bool retire_done(CRAWServer *s)
         struct stream *st = s->streams[i];
         if (!st)
             continue;
-        for (uint32_t k = 0; k < st->nb_slots; k++) {
-            struct slot *sl = &st->slots[k];
-            struct job *j = sl->job;
+        for (;;) {
+            struct slot *sl = oldest_slot(st);
+            struct job *j = sl ? sl->job : NULL;
             CRAWServerResult r;
             cudaError_t e;
             float dev_ms = 0.0f;
 
             if (!j)
-                continue;
+                break;
             e = cudaEventQuery(sl->ev1);
             if (e == cudaErrorNotReady)
-                continue;
+                break;
             progress = true;
             memset(&r, 0, sizeof(r));
             r.user = j->user;
@@ -622,6 +636,7 @@ CRAW_API int craw_server_submit(CRAWServer *s, uint32_t id, const void *src, siz
         return CRAW_ERROR(EINVAL);
     }
     j->t_submit = now_ms();
+    j->seq = s->stats.submitted;
     if (s->q_tail)
         s->q_tail->next = j;
     else

@@ -12,14 +12,71 @@ namespace {
 
 using namespace craw_dev;
 
+/* How a frame's RCD splits into QTW x QTH quad tiles: the interior ones
+ * (rows r_lo..r_hi, columns c_lo..c_hi, all aprons inside the frame) go to
+ * the quad kernel, the ring of the others to the per-pixel kernel, each as
+ * a grid of only its own tiles. */
+struct QuadGrid {
+    int qx, qy;                      /* quad tiles across, down */
+    int r_lo, r_hi, c_lo, c_hi;      /* the interior (empty when hi < lo) */
+    int rows_full, cols_border, mid_rows;
+
+    void init(int w, int h)
+    {
+        qx = (w + QTW - 1) / QTW;
+        qy = (h + QTH - 1) / QTH;
+        /* quad_interior(): x0 >= 6, x0 + QTW + 6 <= w, and the same in y. */
+        c_lo = 1;
+        c_hi = w >= QTW + 6 ? (w - QTW - 6) / QTW : -1;
+        r_lo = 1;
+        r_hi = h >= QTH + 6 ? (h - QTH - 6) / QTH : -1;
+        const bool has_r = r_hi >= r_lo, has_c = c_hi >= c_lo;
+        rows_full = has_r ? r_lo + (qy - 1 - r_hi) : qy;   /* rows with no interior tile */
+        mid_rows = has_r ? r_hi - r_lo + 1 : 0;
+        cols_border = has_c ? c_lo + (qx - 1 - c_hi) : qx;  /* border tiles of the other rows */
+    }
+    int interior_x() const { return c_hi >= c_lo ? c_hi - c_lo + 1 : 0; }
+    int interior_y() const { return r_hi >= r_lo ? r_hi - r_lo + 1 : 0; }
+    int border_quads() const { return rows_full * qx + mid_rows * cols_border; }
+
+    /* Quad tile (col, row) of border tile t. */
+    CRAW_DEV void border(int t, int &col, int &row) const
+    {
+        const bool has_r = r_hi >= r_lo, has_c = c_hi >= c_lo;
+        if (t < rows_full * qx) {
+            const int rr = t / qx;
+            col = t % qx;
+            row = (!has_r || rr < r_lo) ? rr : r_hi + 1 + (rr - r_lo);
+        } else {
+            t -= rows_full * qx;
+            const int rr = t / cols_border, cc = t % cols_border;
+            row = r_lo + rr;
+            col = (!has_c || cc < c_lo) ? cc : c_hi + 1 + (cc - c_lo);
+        }
+    }
+};
+
 __global__ void __launch_bounds__(QNT)
-k_develop_rcd_quads(const CRAWKDevelop k, const CRAWKDevelopIO io)
+k_develop_rcd_quads(const CRAWKDevelop k, const CRAWKDevelopIO io, const QuadGrid g)
 {
     extern __shared__ __align__(16) float smem[];
-    const int x0 = blockIdx.x * QTW, y0 = blockIdx.y * QTH;
-    if (!quad_interior(x0, y0, k.width, k.height))
+    rcd_quad_tile(k, io, (g.c_lo + blockIdx.x) * QTW, (g.r_lo + blockIdx.y) * QTH, smem);
+}
+
+/* The per-pixel RCD on the ring of border quad tiles, BTW x BTH pixels a
+ * CTA (QTW / BTW of them a quad tile). */
+__global__ void __launch_bounds__(256, 8)
+k_develop_rcd_border(const CRAWKDevelop k, const CRAWKDevelopIO io, const QuadGrid g)
+{
+    extern __shared__ __align__(16) float smem[];
+    constexpr int PER = QTW / BTW;
+    static_assert(QTH == BTH, "a border quad tile is one row of per-pixel tiles");
+    int col, row;
+    g.border(blockIdx.x / PER, col, row);
+    const int x0 = col * QTW + (blockIdx.x % PER) * BTW, y0 = row * QTH;
+    if (x0 >= k.width)
         return;
-    rcd_quad_tile(k, io, x0, y0, smem);
+    pixel_tile<kRcd, BTW, BTH, 256>(k, io, x0, y0, smem);
 }
 
 /* Eight CTAs an SM (full occupancy at 256 threads): the bilinear and MHC
@@ -50,11 +107,20 @@ int launch_rcd(const CRAWKDevelop *k, const CRAWKDevelopIO *io, cudaStream_t s)
             return -5;
         attr_set = true;
     }
-    dim3 grid((k->width + QTW - 1) / QTW, (k->height + QTH - 1) / QTH);
-    k_develop_rcd_quads<<<grid, QNT, smem, s>>>(*k, *io);
-    if (cudaGetLastError() != cudaSuccess)
-        return -5;
-    return launch<kRcd, BTW, BTH, 256>(k, io, s);
+    QuadGrid g;
+    g.init(k->width, k->height);
+    if (g.interior_x() > 0 && g.interior_y() > 0) {
+        k_develop_rcd_quads<<<dim3(g.interior_x(), g.interior_y()), QNT, smem, s>>>(*k, *io, g);
+        if (cudaGetLastError() != cudaSuccess)
+            return -5;
+    }
+    if (g.border_quads() > 0) {
+        k_develop_rcd_border<<<g.border_quads() * (QTW / BTW), 256,
+                               PixelSmem<kRcd, BTW, BTH, 256>::floats * sizeof(float), s>>>(*k, *io, g);
+        if (cudaGetLastError() != cudaSuccess)
+            return -5;
+    }
+    return 0;
 }
 
 } // namespace
