@@ -60,6 +60,7 @@ BATCH_FLAG_NO_GRAPH = 1 << 21
 
 FRAME_CLAMP_NEGATIVE = 1 << 0
 FRAME_NO_GAMUT_COMPRESSION = 1 << 2
+FRAME_HIGHLIGHT_RECONSTRUCTION = 1 << 3
 FRAME_TEMPORAL_RESET = 1 << 4
 
 AWB_BINS = 128

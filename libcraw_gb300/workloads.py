@@ -192,3 +192,20 @@ def batch_mix(scale: int = 1) -> list[BatchFrame]:
                               40040 + i, a, b))
     return out
 
+
+
+def highlight_frame(width: int, height: int, seed: int, gain: float = 2.5,
+                    lamps: int = 3) -> np.ndarray:
+    """A synthetic mosaic whose highlights clip: the seeded scene's signal
+    above black raised by `gain`, plus `lamps` bright discs, clipped at the
+    white level (the input of the highlight reconstruction)."""
+    m = synth_frame(width, height, seed, rects=16, zone_plates=1, noise_a_dn=2.0, noise_b_dn=16.0)
+    v = (m.astype(np.float32) - BLACK_DN) * gain
+    rng = np.random.default_rng(seed + 17)
+    yy, xx = np.mgrid[0:height, 0:width]
+    for _ in range(lamps):
+        cx, cy = rng.uniform(0, width), rng.uniform(0, height)
+        r = rng.uniform(0.03, 0.12) * min(width, height)
+        d = np.hypot(xx - cx, yy - cy)
+        v += np.clip(1.0 - d / r, 0.0, 1.0) * RANGE_DN * rng.uniform(1.0, 3.0)
+    return np.clip(np.rint(v + BLACK_DN), 0, WHITE_DN).astype(np.uint16)

@@ -389,6 +389,35 @@ ORC_API int orc_awb_histogram(const float *rgb, uint32_t width, uint32_t height,
     return 0;
 }
 
+/* Rounds a float to the nearest binary16 value, ties to even, returned as a
+ * float: the storage format of the rebuilt highlight mosaic (reference
+ * lib/ref/ref.h:20-57 rounds the same way; magnitudes beyond the half range
+ * do not occur there). */
+static inline float orc_to_half(float f)
+{
+    uint32_t b, sign, mag, keep, rem;
+
+    memcpy(&b, &f, sizeof(b));
+    sign = b & 0x80000000u;
+    mag = b & 0x7FFFFFFFu;
+    if (mag == 0 || mag >= 0x7F800000u)
+        return f;
+    if ((int)(mag >> 23) - 127 < -14) {
+        /* A half subnormal: a multiple of 2^-24. */
+        float q = rintf(fabsf(f) * 16777216.0f) / 16777216.0f;
+        return sign ? -q : q;
+    }
+    /* Ten mantissa bits kept, the other thirteen rounded to nearest even;
+     * a carry out of the mantissa moves into the exponent. */
+    keep = mag >> 13;
+    rem = mag & 0x1FFFu;
+    if (rem > 0x1000u || (rem == 0x1000u && (keep & 1u)))
+        keep++;
+    b = sign | (keep << 13);
+    memcpy(&f, &b, sizeof(f));
+    return f;
+}
+
 /* ------------------------------------------------- the two instantiations */
 
 static inline float orc_mstore_f32(double x) { return (float)x; }
@@ -427,6 +456,13 @@ static inline double orc_mstore_f64(double x) { return x; }
 #undef ORC_CD_RANGE_K
 #undef ORC_CD_CHROMA_K
 #undef ORC_CD_RANGE_EPS
+#undef ORC_HL_U_LO
+#undef ORC_HL_U_HI
+#undef ORC_HL_EPS
+#undef ORC_HL_LOG_MAX
+#undef ORC_HL_W_SAT
+#undef ORC_HL_DILATE
+#undef ORC_HL_LEVELS
 
 #define R double
 #define SFX(n) ORC_API_F64(n)

@@ -41,6 +41,8 @@ int orc_awb_histogram(const float *rgb, uint32_t width, uint32_t height, size_t 
                                  float alpha_max, const R *prev, R *next,                 \
                                  uint16_t *out, size_t out_stride);                       \
     int orc_chroma_denoise_##S(R *rgb, uint32_t w, uint32_t h, float strength);           \
+    int orc_highlights_##S(const uint16_t *bayer, uint32_t w, uint32_t h, size_t stride,   \
+                           const CRAWProfile *profile, const float wb[3], R *out);        \
     int orc_color_##S(R *rgb, uint32_t w, uint32_t h, const CRAWFrameParams *fp,          \
                       int out_space);                                                     \
     int orc_process_##S(const uint16_t *bayer, uint32_t w, uint32_t h, size_t stride,     \

@@ -759,6 +759,258 @@ ORC_API int SFX(orc_color)(R *rgb, uint32_t width, uint32_t height,
     return 0;
 }
 
+/* ------------------------------------------------ highlight reconstruction */
+
+/* The reference's constants, lib/ref/ref_highlight.c:16-21. */
+#define ORC_HL_U_LO ((R)0.92f)
+#define ORC_HL_U_HI ((R)0.98f)
+#define ORC_HL_EPS ((R)1e-4f)
+#define ORC_HL_LOG_MAX ((R)2.0f)
+#define ORC_HL_W_SAT ((R)1.0f)
+#define ORC_HL_DILATE 3
+#define ORC_HL_LEVELS 16
+
+/* Channel of CFA site s (RGGB: R, Gr, Gb, B). */
+static inline int SFX(orc_hl_chan)(int s) { return s == 0 ? 0 : (s == 3 ? 2 : 1); }
+
+static inline R SFX(orc_hl_clampr)(R v, R lo, R hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+/* smoothstep(e0, e1, v): reference lib/ref/ref_highlight.c:41-47. */
+static inline R SFX(orc_hl_smooth)(R e0, R e1, R v)
+{
+    R t = SFX(orc_hl_clampr)((v - e0) / (e1 - e0), (R)0, (R)1);
+    return t * t * ((R)3 - (R)2 * t);
+}
+
+/* One pyramid level: w x h texels of (c0, c1, weight). */
+struct SFX(orc_hl_level) {
+    int w, h;
+    R *t;
+};
+
+/* A level's colour at texel (x, y) clamped to its edge; the top level
+ * still holds sums and is normalised here (ref_highlight.c:57-70). */
+static void SFX(orc_hl_texel)(const struct SFX(orc_hl_level) *l, int x, int y, int top, R out[2])
+{
+    x = x < 0 ? 0 : (x >= l->w ? l->w - 1 : x);
+    y = y < 0 ? 0 : (y >= l->h ? l->h - 1 : y);
+    const R *t = &l->t[((size_t)y * l->w + x) * 3];
+    if (top) {
+        out[0] = t[2] > (R)0 ? t[0] / t[2] : (R)0;
+        out[1] = t[2] > (R)0 ? t[1] / t[2] : (R)0;
+    } else {
+        out[0] = t[0];
+        out[1] = t[1];
+    }
+}
+
+/* Bilinear at (px, py) in texel coordinates, x mixed first
+ * (ref_highlight.c:74-93). */
+static void SFX(orc_hl_sample)(const struct SFX(orc_hl_level) *l, R px, R py, int top, R out[2])
+{
+    R fx0 = R_FLOOR(px), fy0 = R_FLOOR(py), fx = px - fx0, fy = py - fy0;
+    int x0 = (int)fx0, y0 = (int)fy0;
+    R c00[2], c10[2], c01[2], c11[2];
+    SFX(orc_hl_texel)(l, x0, y0, top, c00);
+    SFX(orc_hl_texel)(l, x0 + 1, y0, top, c10);
+    SFX(orc_hl_texel)(l, x0, y0 + 1, top, c01);
+    SFX(orc_hl_texel)(l, x0 + 1, y0 + 1, top, c11);
+    for (int i = 0; i < 2; i++) {
+        R a = c00[i] * ((R)1 - fx) + c10[i] * fx;
+        R b = c01[i] * ((R)1 - fx) + c11[i] * fx;
+        out[i] = a * ((R)1 - fy) + b * fy;
+    }
+}
+
+/* The rebuilt, balanced mosaic of a frame whose highlights clipped:
+ * reference lib/ref/ref_highlight.c:95-335 (DESIGN 18). Every site gets
+ * u * wb of its channel; sites near the clip (a > 0) are lifted toward the
+ * level their unclipped neighbours and the colour field predict. The
+ * colour field is a pyramid of log-chroma averages of the unclipped
+ * quads, pulled up to 1x1 and pushed back down. Output rounded to fp16. */
+ORC_API int SFX(orc_highlights)(const uint16_t *bayer, uint32_t width, uint32_t height,
+                                size_t stride, const CRAWProfile *profile, const float wb[3],
+                                R *out)
+{
+    struct SFX(orc_hl_level) lv[ORC_HL_LEVELS];
+    const int w = (int)width, h = (int)height, qw = w / 2, qh = h / 2;
+    int nl = 0, ret = 0;
+    R *uv, *av, *qa;
+
+    if (!bayer || !profile || !wb || !out)
+        return -EINVAL;
+    if (width < 8 || height < 8 || (width & 1) || (height & 1) || stride < width)
+        return -EINVAL;
+    memset(lv, 0, sizeof(lv));
+    uv = malloc((size_t)w * h * sizeof(R));
+    av = malloc((size_t)w * h * sizeof(R));
+    qa = malloc((size_t)qw * qh * sizeof(R));
+    if (!uv || !av || !qa) {
+        ret = -ENOMEM;
+        goto done;
+    }
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            const int s = (y & 1) * 2 + (x & 1);
+            const R inv = (R)1.0f / ((R)profile->white_level[s] - (R)profile->black_level[s]);
+            const R raw = (R)bayer[(size_t)y * stride + x] * (R)(1.0f / 65535.0f);
+            const R u = (raw - (R)profile->black_level[s]) * inv;
+            uv[(size_t)y * w + x] = u;
+            av[(size_t)y * w + x] = SFX(orc_hl_smooth)(ORC_HL_U_LO, ORC_HL_U_HI, u);
+        }
+    for (int qy = 0; qy < qh; qy++)
+        for (int qx = 0; qx < qw; qx++) {
+            R m = 0;
+            for (int s = 0; s < 4; s++) {
+                R a = av[(size_t)(2 * qy + (s >> 1)) * w + 2 * qx + (s & 1)];
+                m = a > m ? a : m;
+            }
+            qa[(size_t)qy * qw + qx] = m;
+        }
+    /* Level sizes: 4x4 pixels a texel at level 0, halving (rounded up) to 1x1. */
+    for (int lw = (w + 3) / 4, lh = (h + 3) / 4;; lw = (lw + 1) / 2, lh = (lh + 1) / 2) {
+        if (nl == ORC_HL_LEVELS) {
+            ret = -EINVAL;
+            goto done;
+        }
+        lv[nl].w = lw;
+        lv[nl].h = lh;
+        if (!(lv[nl].t = calloc((size_t)lw * lh * 3, sizeof(R)))) {
+            ret = -ENOMEM;
+            goto done;
+        }
+        nl++;
+        if (lw == 1 && lh == 1)
+            break;
+    }
+    /* Level 0: the log chroma of each unclipped quad, weighted by how far
+     * it is from every clip within ORC_HL_DILATE quads and how bright it is. */
+    for (int by = 0; by < lv[0].h; by++)
+        for (int bx = 0; bx < lv[0].w; bx++) {
+            R acc[3] = { 0, 0, 0 };
+            for (int j = 0; j < 2; j++)
+                for (int i = 0; i < 2; i++) {
+                    const int qx = 2 * bx + i, qy = 2 * by + j;
+                    R amax = 0, umax = 0, rgb[3] = { 0, 0, 0 };
+                    if (qx >= qw || qy >= qh)
+                        continue;
+                    for (int dy = -ORC_HL_DILATE; dy <= ORC_HL_DILATE; dy++)
+                        for (int dx = -ORC_HL_DILATE; dx <= ORC_HL_DILATE; dx++) {
+                            const int nx = qx + dx, ny = qy + dy;
+                            if (nx < 0 || ny < 0 || nx >= qw || ny >= qh)
+                                continue;
+                            const R q = qa[(size_t)ny * qw + nx];
+                            amax = q > amax ? q : amax;
+                        }
+                    for (int s = 0; s < 4; s++) {
+                        const R u = uv[(size_t)(2 * qy + (s >> 1)) * w + 2 * qx + (s & 1)];
+                        const int c = SFX(orc_hl_chan)(s);
+                        rgb[c] += u * (R)wb[c];
+                        umax = u > umax ? u : umax;
+                    }
+                    rgb[1] *= (R)0.5f;
+                    const R m = umax < (R)1 ? umax : (R)1;
+                    const R wq = ((R)1 - amax) * m * m;
+                    const R g = rgb[1] > ORC_HL_EPS ? rgb[1] : ORC_HL_EPS;
+                    const R r = SFX(orc_hl_clampr)(R_LOG((rgb[0] > ORC_HL_EPS ? rgb[0] : ORC_HL_EPS) / g),
+                                                   -ORC_HL_LOG_MAX, ORC_HL_LOG_MAX);
+                    const R b = SFX(orc_hl_clampr)(R_LOG((rgb[2] > ORC_HL_EPS ? rgb[2] : ORC_HL_EPS) / g),
+                                                   -ORC_HL_LOG_MAX, ORC_HL_LOG_MAX);
+                    acc[0] += wq * r;
+                    acc[1] += wq * b;
+                    acc[2] += wq;
+                }
+            memcpy(&lv[0].t[((size_t)by * lv[0].w + bx) * 3], acc, sizeof(acc));
+        }
+    /* Pull: each texel the sum of its (up to) four children. */
+    for (int l = 0; l + 1 < nl; l++) {
+        const struct SFX(orc_hl_level) *f = &lv[l];
+        struct SFX(orc_hl_level) *c = &lv[l + 1];
+        for (int y = 0; y < c->h; y++)
+            for (int x = 0; x < c->w; x++) {
+                R acc[3] = { 0, 0, 0 };
+                for (int dy = 0; dy < 2; dy++)
+                    for (int dx = 0; dx < 2; dx++) {
+                        const int fx = 2 * x + dx, fy = 2 * y + dy;
+                        if (fx >= f->w || fy >= f->h)
+                            continue;
+                        for (int k = 0; k < 3; k++)
+                            acc[k] += f->t[((size_t)fy * f->w + fx) * 3 + k];
+                    }
+                memcpy(&c->t[((size_t)y * c->w + x) * 3], acc, sizeof(acc));
+            }
+    }
+    /* Push: from under the top to level 0, each texel blended from the
+     * coarser level's bilinear colour toward its own mean by its weight. */
+    for (int l = nl - 2; l >= 0; l--) {
+        struct SFX(orc_hl_level) *f = &lv[l];
+        const struct SFX(orc_hl_level) *c = &lv[l + 1];
+        const int top = l + 2 == nl;
+        for (int y = 0; y < f->h; y++)
+            for (int x = 0; x < f->w; x++) {
+                R *t = &f->t[((size_t)y * f->w + x) * 3], up[2];
+                SFX(orc_hl_sample)(c, ((R)x + (R)0.5f) * (R)0.5f - (R)0.5f,
+                                   ((R)y + (R)0.5f) * (R)0.5f - (R)0.5f, top, up);
+                if (t[2] > (R)0) {
+                    const R s = t[2] / ORC_HL_W_SAT < (R)1 ? t[2] / ORC_HL_W_SAT : (R)1;
+                    t[0] = up[0] + s * (t[0] / t[2] - up[0]);
+                    t[1] = up[1] + s * (t[1] / t[2] - up[1]);
+                } else {
+                    t[0] = up[0];
+                    t[1] = up[1];
+                }
+            }
+    }
+    /* Fill. */
+    for (int y = 0; y < h; y++)
+        for (int x = 0; x < w; x++) {
+            const size_t o = (size_t)y * w + x;
+            const int c = SFX(orc_hl_chan)((y & 1) * 2 + (x & 1));
+            const R xc = uv[o] * (R)wb[c], a = av[o];
+            R res = xc;
+            if (a > (R)0) {
+                R sum[3] = { 0, 0, 0 }, n[3] = { 0, 0, 0 }, am[3] = { 0, 0, 0 }, lf[2], lrho[3];
+                SFX(orc_hl_sample)(&lv[0], (R)(x >> 1) * (R)0.5f - (R)0.25f,
+                                   (R)(y >> 1) * (R)0.5f - (R)0.25f, 0, lf);
+                lrho[0] = lf[0];
+                lrho[1] = 0;
+                lrho[2] = lf[1];
+                for (int dy = -1; dy <= 1; dy++)
+                    for (int dx = -1; dx <= 1; dx++) {
+                        const int nx = SFX(orc_mirror)(x + dx, w), ny = SFX(orc_mirror)(y + dy, h);
+                        const int k = SFX(orc_hl_chan)((ny & 1) * 2 + (nx & 1));
+                        const size_t no = (size_t)ny * w + nx;
+                        if (k == c)
+                            continue;
+                        sum[k] += uv[no] * (R)wb[k];
+                        n[k] += (R)1;
+                        am[k] = av[no] > am[k] ? av[no] : am[k];
+                    }
+                const int k1 = c == 0 ? 1 : 0, k2 = c == 2 ? 1 : 2;
+                const R a1 = (R)1 - am[k1], a2 = (R)1 - am[k2];
+                const R m1 = sum[k1] / n[k1], m2 = sum[k2] / n[k2];
+                const R l1 = R_LOG(m1 > ORC_HL_EPS ? m1 : ORC_HL_EPS) - lrho[k1];
+                const R l2 = R_LOG(m2 > ORC_HL_EPS ? m2 : ORC_HL_EPS) - lrho[k2];
+                const R lc = R_LOG(xc > ORC_HL_EPS ? xc : ORC_HL_EPS) - lrho[c];
+                const R A = a1 + a2;
+                const R lmax = lc > (l1 > l2 ? l1 : l2) ? lc : (l1 > l2 ? l1 : l2);
+                const R lfull = R_EXP(lmax);
+                const R lpart = A > (R)0 ? R_EXP((a1 * l1 + a2 * l2) / A) : lfull;
+                const R L = lfull + (A < (R)1 ? A : (R)1) * (lpart - lfull);
+                const R lift = L * R_EXP(lrho[c]) - xc;
+                res = xc + a * (lift > (R)0 ? lift : (R)0);
+            }
+            out[o] = (R)orc_to_half((float)res);
+        }
+done:
+    for (int i = 0; i < nl; i++)
+        free(lv[i].t);
+    free(uv);
+    free(av);
+    free(qa);
+    return ret;
+}
+
 /* --------------------------------------------------------- whole frame */
 
 /* One frame through the chain, reference lib/ref/ref_color.c:91-230,
@@ -809,8 +1061,23 @@ ORC_API int SFX(orc_process)(const uint16_t *bayer, uint32_t width, uint32_t hei
         ret = orc_profile_eval(fp->profile, fp->wb_mode, &fp->illuminant, &par);
         if (ret < 0)
             goto done;
-        ret = SFX(orc_debayer_wb)(bayer, width, height, stride, fp->profile, par.wb,
-                                  params->debayer, out);
+        if ((params->flags & CRAW_PIPELINE_FLAG_HIGHLIGHT_RECONSTRUCTION) &&
+            (fp->flags & CRAW_FRAME_FLAG_HIGHLIGHT_RECONSTRUCTION)) {
+            /* The rebuilt mosaic replaces the prep and its clip
+             * (ref_color.c:146-160). */
+            R *v = malloc((size_t)width * height * sizeof(R));
+            if (!v) {
+                ret = -ENOMEM;
+                goto done;
+            }
+            ret = SFX(orc_highlights)(bayer, width, height, stride, fp->profile, par.wb, v);
+            if (ret >= 0)
+                ret = SFX(orc_debayer_mosaic)(v, width, height, params->debayer, out);
+            free(v);
+        } else {
+            ret = SFX(orc_debayer_wb)(bayer, width, height, stride, fp->profile, par.wb,
+                                      params->debayer, out);
+        }
         if (ret < 0)
             goto done;
     }

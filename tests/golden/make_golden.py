@@ -42,6 +42,9 @@ PROCESS_CASES = [
      {"wb_mode": L.WB_REBALANCE, "illuminant": (3900.0, 0.03)}),
 ]
 
+#: Highlight reconstruction cases: (name, w, h, seed, white balance).
+HL_CASES = [("as_shot", 96, 64, 401, (2.0, 1.0, 1.5)), ("warm", 130, 78, 402, (1.7, 1.0, 2.2))]
+
 #: A white balance / matrix table of this project's own, for the rebalance cases.
 WB_KNOTS = [(2500.0, (1.05, 1.0, 3.10)), (4000.0, (1.55, 1.0, 2.05)), (5500.0, (2.00, 1.0, 1.50)),
             (7500.0, (2.40, 1.0, 1.25))]
@@ -107,6 +110,19 @@ def main() -> None:
     cnt, wgt, brt = ref.awb_histogram(rgb, W.WB)
     out["awb/rgb"] = rgb
     out["awb/count"], out["awb/weight"], out["awb/weight_bright"] = cnt, wgt, brt
+
+    # Highlight reconstruction (lib/ref/ref_highlight.c): the rebuilt mosaic,
+    # and a whole frame through it.
+    for name, w, h, seed, wb in HL_CASES:
+        m = W.highlight_frame(w, h, seed)
+        out[f"highlights/{name}/in"] = m
+        out[f"highlights/{name}/out"] = ref.highlights(m, prof, wb)
+    m = W.highlight_frame(64, 48, 404)
+    pp = L.pipeline_params(64, 48, debayer=L.DEBAYER_RCD, out_space=L.CS_ACES_AP1,
+                           flags=L.FLAG_HIGHLIGHT_RECONSTRUCTION, out_format=L.FORMAT_RGBA32F)
+    fp = L.frame_params(prof, flags=L.FRAME_HIGHLIGHT_RECONSTRUCTION)
+    out["highlights/process/in"] = m
+    out["highlights/process/out"] = ref.process(m, pp, fp)
 
     # Host constants.
     for cs in range(7):

@@ -47,6 +47,7 @@ class Oracle:
             _sig(lib, f"orc_debayer_mosaic_{s}", i32, [vp, u32, u32, i32, vp])
             _sig(lib, f"orc_chroma_denoise_{s}", i32, [vp, u32, u32, f32])
             _sig(lib, f"orc_color_{s}", i32, [vp, u32, u32, P(L.FrameParams), i32])
+            _sig(lib, f"orc_highlights_{s}", i32, [vp, u32, u32, sz, P(L.Profile), P(C.c_float * 3), vp])
         _sig(lib, "orc_awb_histogram", i32, [vp, u32, u32, sz, i32, P(C.c_float * 3), vp, vp, vp])
         _sig(lib, "orc_profile_eval", i32, [P(L.Profile), i32, P(L.Illuminant), P(L.ColorParams)])
         _sig(lib, "orc_colorspace_from_xyz_f", i32, [i32, P(C.c_float * 9)])
@@ -88,6 +89,16 @@ class Oracle:
         out = np.ascontiguousarray(rgba, self._dt(s)).copy()
         h, w, _ = out.shape
         ret = getattr(self.lib, f"orc_chroma_denoise_{s}")(out.ctypes.data, w, h, strength)
+        assert ret == 0, ret
+        return out
+
+    def highlights(self, bayer, profile, wb, s="f32"):
+        """The rebuilt, balanced mosaic (values rounded to fp16)."""
+        h, w = bayer.shape
+        out = np.zeros((h, w), self._dt(s))
+        ret = getattr(self.lib, f"orc_highlights_{s}")(bayer.ctypes.data, w, h, bayer.strides[0] // 2,
+                                                      C.byref(profile), C.byref((C.c_float * 3)(*wb)),
+                                                      out.ctypes.data)
         assert ret == 0, ret
         return out
 
@@ -161,6 +172,14 @@ class Reference:
         out = np.ascontiguousarray(rgba, np.float32).copy()
         h, w, _ = out.shape
         assert self.lib.craw_ref_chroma_denoise(out.ctypes.data, w, h, strength) == 0
+        return out
+
+    def highlights(self, bayer, profile, wb, s="f32"):
+        h, w = bayer.shape
+        out = np.zeros((h, w), np.float32)
+        _sig(self.lib, "craw_ref_highlights", i32, [vp, u32, u32, sz, P(L.Profile), P(C.c_float * 3), vp])
+        assert self.lib.craw_ref_highlights(bayer.ctypes.data, w, h, bayer.strides[0] // 2, C.byref(profile),
+                                            C.byref((C.c_float * 3)(*wb)), out.ctypes.data) == 0
         return out
 
     def color(self, rgba, fp, out_space, s="f32"):

@@ -48,6 +48,44 @@ def test_temporal_golden():
     assert np.array_equal(clean, GOLD["temporal_only/clean"])
 
 
+@pytest.mark.parametrize("case", MG.HL_CASES, ids=[c[0] for c in MG.HL_CASES])
+def test_highlights_golden(case):
+    """The highlight reconstruction restated (lib/ref/ref_highlight.c): the
+    rebuilt fp16 mosaic bit for bit, and the double run within fp16
+    rounding of it."""
+    name, w, h, seed, wb = case
+    prof = MG.golden_profile()
+    m = GOLD[f"highlights/{name}/in"]
+    got = orc.highlights(m, prof, wb, "f32")
+    assert np.array_equal(got, GOLD[f"highlights/{name}/out"])
+    # The frame is clipped and the pass lifted it past the clip point.
+    assert (m == W.WHITE_DN).mean() > 0.05 and got.max() > 1.2
+    d = orc.highlights(m, prof, wb, "f64")
+    assert np.max(np.abs(d - got) / np.maximum(np.abs(got), 1e-3)) < 2e-3
+
+
+def test_highlights_process_golden():
+    prof = MG.golden_profile()
+    m = GOLD["highlights/process/in"]
+    pp = L.pipeline_params(64, 48, debayer=L.DEBAYER_RCD, out_space=L.CS_ACES_AP1,
+                           flags=L.FLAG_HIGHLIGHT_RECONSTRUCTION, out_format=L.FORMAT_RGBA32F)
+    fp = L.frame_params(prof, flags=L.FRAME_HIGHLIGHT_RECONSTRUCTION)
+    assert np.array_equal(orc.process(m, pp, fp, "f32"), GOLD["highlights/process/out"])
+    # The frame flag alone switches the pass: without it, the plain prep.
+    fp0 = L.frame_params(prof)
+    assert not np.array_equal(orc.process(m, pp, fp0, "f32"), GOLD["highlights/process/out"])
+
+
+@needs_ref
+def test_highlights_against_reference_build():
+    prof = MG.golden_profile()
+    ref = Reference()
+    for seed, (w, h) in enumerate([(64, 48), (98, 66), (160, 120), (8, 8)]):
+        m = W.highlight_frame(w, h, 500 + seed)
+        for wb in ((2.0, 1.0, 1.5), (1.3, 1.0, 2.6)):
+            assert np.array_equal(orc.highlights(m, prof, wb, "f32"), ref.highlights(m, prof, wb)), (w, h, wb)
+
+
 def test_awb_golden():
     rgb = GOLD["awb/rgb"]
     for impl in (orc.awb_histogram(rgb, W.WB), L.awb_histogram_from_rgb(rgb, W.WB)):
