@@ -20,6 +20,8 @@
  * VK_FORMAT_R32G32B32A32_SFLOAT). */
 typedef enum CRAWFormat {
     CRAW_FORMAT_R16_UNORM = 70,   /* Bayer mosaic, one uint16 per sample */
+    CRAW_FORMAT_R16F      = 76,   /* one half float per sample (VK_FORMAT_R16_SFLOAT): the
+                                   * rebuilt highlight mosaic, read back for tests only */
     CRAW_FORMAT_RGBA16F   = 97,   /* four IEEE half floats per pixel */
     CRAW_FORMAT_RGBA32F   = 109,  /* four IEEE floats per pixel */
 } CRAWFormat;

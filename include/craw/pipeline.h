@@ -45,7 +45,12 @@ enum CRAWDebayer {
 #define CRAW_PIPELINE_FLAG_LENS                     (1 << 2)  /* not built: ENOTSUP */
 #define CRAW_PIPELINE_FLAG_FALSE_COLOR              (1 << 3)  /* not built: ENOTSUP */
 #define CRAW_PIPELINE_FLAG_CHROMA_DENOISE           (1 << 4)
-#define CRAW_PIPELINE_FLAG_HIGHLIGHT_RECONSTRUCTION (1 << 5)  /* not built: ENOTSUP */
+/* Rebuild clipped highlights before the debayer (reference pipeline.h:86-103):
+ * a quarter-resolution colour field of the unclipped neighbourhood and its
+ * pyramid predict the channels that clipped; the rebuilt mosaic (fp16) may
+ * exceed the balanced clip point. Switched per frame by
+ * CRAW_FRAME_FLAG_HIGHLIGHT_RECONSTRUCTION. Not with CRAW_IMPL_PLAIN. */
+#define CRAW_PIPELINE_FLAG_HIGHLIGHT_RECONSTRUCTION (1 << 5)
 #define CRAW_PIPELINE_FLAG_DEFRINGE                 (1 << 6)  /* not built: ENOTSUP */
 #define CRAW_PIPELINE_FLAG_TEMPORAL_DENOISE         (1 << 7)
 #define CRAW_PIPELINE_FLAG_SHARPEN                  (1 << 8)  /* not built: ENOTSUP */
@@ -53,8 +58,10 @@ enum CRAWDebayer {
 
 /* Extension, no counterpart in the reference: keep the camera RGB
  * intermediate (after the debayer and the chroma denoise, exactly what the
- * AWB histogram and the colour stage read) and the denoised mosaic in
- * device memory where craw_pipeline_get_intermediate() can hand them out.
+ * AWB histogram and the colour stage read) and the mosaic the debayer read
+ * (the denoised R16_UNORM one, or the rebuilt R16F one after a highlight
+ * reconstruction) in device memory where craw_pipeline_get_intermediate()
+ * can hand them out.
  * Without it the fused kernels never write the intermediate at all. */
 #define CRAW_PIPELINE_FLAG_KEEP_INTERMEDIATE        (1 << 16)
 
@@ -113,7 +120,7 @@ typedef struct CRAWPipelineParams {
 #define CRAW_FRAME_FLAG_CLAMP_NEGATIVE           (1 << 0)
 #define CRAW_FRAME_FLAG_LENS_KEEP_ALL            (1 << 1)  /* ignored */
 #define CRAW_FRAME_FLAG_NO_GAMUT_COMPRESSION     (1 << 2)
-#define CRAW_FRAME_FLAG_HIGHLIGHT_RECONSTRUCTION (1 << 3)  /* ignored */
+#define CRAW_FRAME_FLAG_HIGHLIGHT_RECONSTRUCTION (1 << 3)  /* needs the pipeline flag */
 #define CRAW_FRAME_FLAG_TEMPORAL_RESET           (1 << 4)
 
 /* Per-frame settings; 264 bytes, field for field the reference's

@@ -39,6 +39,7 @@ DEBAYER_BILINEAR, DEBAYER_MHC, DEBAYER_RCD = 0, 1, 2
 (CS_XYZ_D65, CS_BT709, CS_BT2020, CS_P3D65, CS_V_GAMUT, CS_ACES_AP0,
  CS_ACES_AP1) = range(7)
 FORMAT_R16_UNORM, FORMAT_RGBA16F, FORMAT_RGBA32F = 70, 97, 109
+FORMAT_R16F = 76
 WB_AS_SHOT, WB_REBALANCE = 0, 1
 STORAGE_FP32, STORAGE_FP16 = 0, 1
 IMPL_FUSED, IMPL_PLAIN = 0, 1

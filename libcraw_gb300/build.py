@@ -41,6 +41,9 @@ HOST_CFLAGS = ["-std=c2x", "-O2", "-fPIC", "-fvisibility=hidden", "-Wall", "-Wex
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fvisibility=hidden", f"-I{ROOT / 'include'}",
               "-diag-suppress", "177"]
+# The highlight pass decides per site whether to lift it by comparing
+# values with 0: built like the oracle, without multiply-add contraction.
+NVCC_FILE_FLAGS = {"highlight": ["-fmad=false"]}
 
 
 def _headers(*dirs: Path) -> float:
@@ -81,7 +84,8 @@ def build(verbose: bool = False, with_reference: bool | None = None) -> dict[str
     for cu in sorted((CSRC / "kernels").glob("*.cu")):
         o = OBJ / (cu.stem + ".cu.o")
         objs.append(o)
-        jobs.append((o, [NVCC, *NVCC_FLAGS, "-c", str(cu), "-o", str(o)], [cu]))
+        jobs.append((o, [NVCC, *NVCC_FLAGS, *NVCC_FILE_FLAGS.get(cu.stem, []), "-c", str(cu), "-o", str(o)],
+                     [cu]))
 
     todo = [j for j in jobs if _stale(j[0], j[2], hdr)]
     workers = max(1, min(len(todo), os.cpu_count() or 4))

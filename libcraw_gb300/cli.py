@@ -7,6 +7,10 @@ pipeline on frames of a given size (`cineraw --bench`, tools/cineraw.c:
     python -m libcraw_gb300.cli bench --width W --height H [--frames N] [options]
     python -m libcraw_gb300.cli synth OUT.raw --width W --height H [--seed S]
 
+Options include the stages (--denoise, --temporal, --chroma strengths,
+--highlights) and, for synthetic frames, --scene highlights: the scene at
+2.5x exposure under three lamps, a third of its sites near the clip.
+
 A mosaic dump is W x H native-endian uint16 samples, rows top to bottom,
 no header (the reference's test frames, tests/test_pipeline.c:5519-5562).
 A PFM file is "PF\\n<w> <h>\\n-1.0\\n" followed by little-endian float32
@@ -88,6 +92,9 @@ def params(args, width: int, height: int) -> tuple[L.PipelineParams, L.FramePara
     if args.denoise > 0 or args.temporal > 0:
         rng = args.white - args.black
         kw["noise_override"] = (args.noise[0] / rng, args.noise[1] / (rng * rng))
+    if args.highlights:
+        flags |= L.FLAG_HIGHLIGHT_RECONSTRUCTION
+        kw["flags"] = L.FRAME_HIGHLIGHT_RECONSTRUCTION
     pp = L.pipeline_params(width, height, debayer=DEBAYERS[args.debayer], out_space=SPACES[args.space],
                            flags=flags, out_format=L.FORMAT_RGBA32F,
                            storage=L.STORAGE_FP16 if args.fp16 else L.STORAGE_FP32)
@@ -134,8 +141,7 @@ def cmd_bench(args) -> int:
     if args.input:
         src = [read_raw(args.input, args.width, args.height)]
     else:
-        src = [W.synth_frame(args.width, args.height, 4242 + i, noise_a_dn=args.noise[0],
-                             noise_b_dn=args.noise[1]) for i in range(4)]
+        src = [scene(args, 4242 + i) for i in range(4)]
     h, w = src[0].shape
     pp, fp, _ = params(args, w, h)
     ctx = L.Context(args.device)
@@ -166,9 +172,17 @@ def cmd_bench(args) -> int:
     return 0
 
 
+def scene(args, seed: int) -> np.ndarray:
+    """A seeded synthetic mosaic: the benchmark scene, or with --scene
+    highlights the scene at 2.5x exposure under three lamps (a third of
+    the sites near or at the clip)."""
+    if args.scene == "highlights":
+        return W.highlight_frame(args.width, args.height, seed)
+    return W.synth_frame(args.width, args.height, seed, noise_a_dn=args.noise[0], noise_b_dn=args.noise[1])
+
+
 def cmd_synth(args) -> int:
-    m = W.synth_frame(args.width, args.height, args.seed, noise_a_dn=args.noise[0], noise_b_dn=args.noise[1])
-    m.astype(np.uint16).tofile(args.output)
+    scene(args, args.seed).astype(np.uint16).tofile(args.output)
     return 0
 
 
@@ -181,6 +195,8 @@ def parser() -> argparse.ArgumentParser:
         p.add_argument("--height", type=int, required=True)
         p.add_argument("--noise", type=float, nargs=2, default=(4.0, 40.0), metavar=("A_DN", "B_DN"),
                        help="noise model var = a*signal + b in DN (synthesis and the denoise)")
+        p.add_argument("--scene", choices=("plain", "highlights"), default="plain",
+                       help="synthetic frames: the benchmark scene, or one whose highlights clip")
         if not need_io:
             return
         p.add_argument("--device", type=int, default=0)
@@ -191,6 +207,8 @@ def parser() -> argparse.ArgumentParser:
         p.add_argument("--chroma", type=float, default=0.0, help="chroma denoise strength (0: off)")
         p.add_argument("--exposure", type=float, default=0.0, help="stops")
         p.add_argument("--fp16", action="store_true", help="FP16 intermediate storage")
+        p.add_argument("--highlights", action="store_true",
+                       help="rebuild clipped highlights before the debayer")
         p.add_argument("--black", type=float, default=W.BLACK_DN, help="black level, 16-bit code")
         p.add_argument("--white", type=float, default=W.WHITE_DN, help="white level, 16-bit code")
         p.add_argument("--wb", type=float, nargs=3, default=W.WB, metavar=("R", "G", "B"),

@@ -19,6 +19,7 @@
  * from a CUDA memory pool (cudaMallocFromPoolAsync on the context's own
  * stream, which is synchronised once at the end of creation).
  */
+#include <float.h>
 #include <math.h>
 #include <pthread.h>
 #include <stdio.h>
@@ -42,12 +43,12 @@ static_assert(sizeof(CRAWCudaInitParams) == 64, "CRAWCudaInitParams size");
 
 #define MAX_STAGES 16
 
-enum { ST_DENOISE, ST_DEVELOP, ST_BLUR, ST_UP, ST_AWB, ST_NB };
+enum { ST_DENOISE, ST_DEVELOP, ST_BLUR, ST_UP, ST_AWB, ST_HL, ST_NB };
 static const char *const stage_names[ST_NB] = {
-    "denoise_nlm", "develop", "chroma_blur", "chroma_up_color", "awb_reduce",
+    "denoise_nlm", "develop", "chroma_blur", "chroma_up_color", "awb_reduce", "highlights",
 };
 static const char *const plain_stage_names[ST_NB] = {
-    "plain_denoise", "plain_develop", "plain_chroma", "plain_chroma", "plain_awb",
+    "plain_denoise", "plain_develop", "plain_chroma", "plain_chroma", "plain_awb", "highlights",
 };
 
 /* One host-visible AWB slot: the three histograms, then the deferred
@@ -67,6 +68,11 @@ struct CRAWPipeline {
     CRAWContext *ctx;
     CRAWPipelineParams params;
     bool has_denoise, has_temporal, has_chroma, awb, profile, keep, plain, fp16;
+    bool has_hl;                 /* highlight reconstruction built */
+    CRAWKHighlight hl;           /* its level sizes (constants filled per frame) */
+    uint16_t *hl_mosaic;         /* the rebuilt mosaic, fp16 */
+    size_t hl_pitch;
+    void *hl_levels;            /* the colour field's pyramid */
     int dn_shape[2], dev_shape;   /* denoise tile shape without / with a history */
 
     /* Device memory. */
@@ -87,7 +93,7 @@ struct CRAWPipeline {
     struct awb_slot slots[4];
     uint32_t nb_slots;
     uint64_t nb_recorded;
-    bool last_denoised;
+    bool last_denoised, last_hl;
 
     struct prof_slot prof[CRAW_PIPELINE_PROFILE_SLOTS];
     uint64_t prof_recorded;
@@ -130,6 +136,7 @@ static void release(CRAWPipeline *p)
     void *bufs[] = {
         p->clean, p->lvl[0], p->lvl[1], p->var[0], p->var[1], p->inter, p->q, p->qf,
         p->awb_rec, p->awb_dev, p->p_v, p->p_scratch, p->p_t, p->p_var,
+        p->hl_mosaic, p->hl_levels,
     };
     cudaSetDevice(ctx->device);
     for (size_t i = 0; i < CRAW_ARRAY_ELEMS(bufs); i++)
@@ -285,7 +292,6 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
                                   CRAWPipeline **out)
 {
     const uint32_t unsupported = CRAW_PIPELINE_FLAG_LENS | CRAW_PIPELINE_FLAG_FALSE_COLOR |
-                                 CRAW_PIPELINE_FLAG_HIGHLIGHT_RECONSTRUCTION |
                                  CRAW_PIPELINE_FLAG_DEFRINGE | CRAW_PIPELINE_FLAG_SHARPEN;
     CRAWPipeline *p;
     uint32_t w, h;
@@ -300,8 +306,13 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
     }
     if (params->flags & unsupported) {
         craw_log(ctx, CRAW_LOG_ERROR, "Pipeline flags 0x%x name stages this library does not "
-                 "build (lens, false colour, highlights, defringe, sharpening)\n",
+                 "build (lens, false colour, defringe, sharpening)\n",
                  params->flags & unsupported);
+        return CRAW_ERROR(ENOTSUP);
+    }
+    if ((params->flags & CRAW_PIPELINE_FLAG_HIGHLIGHT_RECONSTRUCTION) &&
+        params->impl == CRAW_IMPL_PLAIN) {
+        craw_log(ctx, CRAW_LOG_ERROR, "The plain pipeline has no highlight reconstruction\n");
         return CRAW_ERROR(ENOTSUP);
     }
     w = params->width;
@@ -332,6 +343,7 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
     p->has_denoise = params->flags & CRAW_PIPELINE_FLAG_DENOISE;
     p->has_temporal = params->flags & CRAW_PIPELINE_FLAG_TEMPORAL_DENOISE;
     p->has_chroma = params->flags & CRAW_PIPELINE_FLAG_CHROMA_DENOISE;
+    p->has_hl = params->flags & CRAW_PIPELINE_FLAG_HIGHLIGHT_RECONSTRUCTION;
     p->profile = params->flags & CRAW_PIPELINE_FLAG_PROFILE;
     p->keep = params->flags & CRAW_PIPELINE_FLAG_KEEP_INTERMEDIATE;
     p->plain = params->impl == CRAW_IMPL_PLAIN;
@@ -377,6 +389,18 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
     if (p->has_chroma || p->keep || p->plain) {
         size_t bpp = p->fp16 ? 8 : 16;
         if ((ret = alloc_pitched(p, &p->inter, &p->inter_pitch, (size_t)w * bpp, h)) < 0)
+            goto fail;
+    }
+    if (p->has_hl) {
+        /* The rebuilt mosaic (fp16) and the colour field's pyramid: 62 MB
+         * at 5760x3240. */
+        int64_t texels = craw_k_highlight_levels((int32_t)w, (int32_t)h, &p->hl);
+        if (texels < 0) {
+            ret = CRAW_ERROR(EINVAL);
+            goto fail;
+        }
+        if ((ret = alloc_pitched(p, (void **)&p->hl_mosaic, &p->hl_pitch, (size_t)w * 2, h)) < 0 ||
+            (ret = craw_dev_alloc(ctx, &p->hl_levels, (size_t)texels * 16)) < 0)
             goto fail;
     }
     if (p->has_chroma) {
@@ -587,6 +611,41 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
     dio.src = mosaic;
     dio.src_pitch = mosaic_pitch;
     dio.awb = awb;
+
+    /* Highlight reconstruction (reference pipeline.c:2047-2062): the
+     * rebuilt, balanced fp16 mosaic replaces the one the debayer reads, and
+     * the debayer's prep becomes the identity with no clip. */
+    if (p->has_hl && (fp->flags & CRAW_FRAME_FLAG_HIGHLIGHT_RECONSTRUCTION)) {
+        CRAWKHighlight hk = p->hl;
+        CRAWKHighlightIO hio = {
+            .src = mosaic, .src_pitch = mosaic_pitch,
+            .dst = p->hl_mosaic, .dst_pitch = p->hl_pitch,
+            .levels = p->hl_levels,
+        };
+        hk.width = (int32_t)w;
+        hk.height = (int32_t)h;
+        for (int i = 0; i < 4; i++) {
+            hk.black[i] = dk.black[i];
+            hk.inv_range[i] = dk.inv_range[i];
+        }
+        hk.wb[0] = dk.wbs[0];
+        hk.wb[1] = dk.wbs[1];
+        hk.wb[2] = dk.wbs[3];
+        prof_begin(&pc, ST_HL);
+        ret = craw_k_highlights(&hk, &hio, s);
+        prof_end(&pc);
+        if (ret < 0)
+            goto launch_fail;
+        dio.src = p->hl_mosaic;
+        dio.src_pitch = p->hl_pitch;
+        dio.src_f16 = 1;
+        for (int i = 0; i < 4; i++) {
+            dk.black[i] = 0.0f;
+            dk.inv_range[i] = 1.0f;
+            dk.wbs[i] = 1.0f;
+        }
+        dk.clip = FLT_MAX;
+    }
     memset(&ck, 0, sizeof(ck));
     ck.width = (int32_t)w;
     ck.height = (int32_t)h;
@@ -664,6 +723,7 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
     if (p->profile)
         p->prof_recorded++;
     p->last_denoised = denoise;
+    p->last_hl = dio.src_f16;
 
     /* Only now does the temporal state move (reference pipeline.c:2303-2313). */
     if (p->has_temporal) {
@@ -786,9 +846,9 @@ CRAW_API int craw_pipeline_get_intermediate(CRAWPipeline *p, CRAWImage *rgb, CRA
         rgb->height = p->params.height;
     }
     if (mosaic) {
-        mosaic->data = p->last_denoised ? p->clean : NULL;
-        mosaic->pitch = p->clean_pitch;
-        mosaic->format = CRAW_FORMAT_R16_UNORM;
+        mosaic->data = p->last_hl ? (void *)p->hl_mosaic : (p->last_denoised ? p->clean : NULL);
+        mosaic->pitch = p->last_hl ? p->hl_pitch : p->clean_pitch;
+        mosaic->format = p->last_hl ? CRAW_FORMAT_R16F : CRAW_FORMAT_R16_UNORM;
         mosaic->width = p->params.width;
         mosaic->height = p->params.height;
     }

@@ -104,6 +104,8 @@ typedef struct CRAWKAwbOut {
 
 typedef struct CRAWKDevelopIO {
     const uint16_t *src; size_t src_pitch;
+    int32_t src_f16;                                    /* src holds fp16 values already
+                                                         * prepped (the rebuilt highlights) */
     void *dst; size_t dst_pitch; int32_t dst_half;      /* NULL: no colour stage */
     void *inter; size_t inter_pitch;                    /* NULL: not kept */
     void *quarter; size_t quarter_pitch;                /* chroma: block means out */
@@ -140,6 +142,36 @@ int craw_k_chroma_up_color(const CRAWKDevelop *k, const CRAWKChroma *c,
 /* Folds `n` block records into the three 128^2 histograms (zeroed by the
  * caller), through shared-memory histograms with warp-aggregated atomics. */
 int craw_k_awb_reduce(const uint64_t *rec, uint32_t n, uint32_t *hist, cudaStream_t s);
+
+/* ------------------------------------------------------ highlights */
+
+/* The highlight reconstruction of one frame: the mosaic's sites as
+ * u = (raw/65535 - black) * inv_range, their clip ramp a, a pyramid of
+ * log-chroma colour fields from the unclipped quads, and the rebuilt,
+ * balanced mosaic (u * gain, lifted near the clip) as fp16. */
+#define CRAW_K_HL_LEVELS 16
+
+typedef struct CRAWKHighlight {
+    int32_t width, height;           /* mosaic; qw = width / 2, qh = height / 2 */
+    float black[4], inv_range[4];    /* per quad site */
+    float wb[3];                     /* gains of R, G, B */
+    int32_t nb_levels;
+    int32_t lw[CRAW_K_HL_LEVELS], lh[CRAW_K_HL_LEVELS];
+    int64_t off[CRAW_K_HL_LEVELS];   /* float4 offset of each level */
+} CRAWKHighlight;
+
+typedef struct CRAWKHighlightIO {
+    const uint16_t *src; size_t src_pitch;
+    uint16_t *dst; size_t dst_pitch;  /* fp16 bits, balanced mosaic */
+    void *levels;                   /* float4 texels (c0, c1, weight, 0) */
+} CRAWKHighlightIO;
+
+/* Level sizes and offsets of a width x height frame into `k`; returns the
+ * float4 texels of the whole pyramid, or -1 when it needs more than
+ * CRAW_K_HL_LEVELS levels. */
+int64_t craw_k_highlight_levels(int32_t width, int32_t height, CRAWKHighlight *k);
+
+int craw_k_highlights(const CRAWKHighlight *k, const CRAWKHighlightIO *io, cudaStream_t s);
 
 /* ------------------------------------------------------------- batch */
 

@@ -74,7 +74,7 @@ CRAW_DEV void load_prepped(const CRAWKDevelop &k, const CRAWKDevelopIO &io, cons
             y = craw_mirror(y, f.h);
         }
         uint16_t raw = __ldg((const uint16_t *)((const char *)io.src + (size_t)y * io.src_pitch) + x);
-        v.p[i] = craw_prep(k, raw, (y & 1) * 2 + (x & 1));
+        v.p[i] = io.src_f16 ? __half2float(__ushort_as_half(raw)) : craw_prep(k, raw, (y & 1) * 2 + (x & 1));
     }
 }
 
@@ -344,8 +344,14 @@ struct RcdQuads {
             const char *r0 = (const char *)io.src + (size_t)y * io.src_pitch;
             uint32_t a = __ldg(reinterpret_cast<const uint32_t *>(r0) + x / 2);
             uint32_t b = __ldg(reinterpret_cast<const uint32_t *>(r0 + io.src_pitch) + x / 2);
-            float2 top = make_float2(craw_prep(k, (uint16_t)(a & 0xffff), 0), craw_prep(k, (uint16_t)(a >> 16), 1));
-            float2 bot = make_float2(craw_prep(k, (uint16_t)(b & 0xffff), 2), craw_prep(k, (uint16_t)(b >> 16), 3));
+            float2 top, bot;
+            if (io.src_f16) {   /* rebuilt highlights: fp16, already prepped */
+                top = __half22float2(*reinterpret_cast<const __half2 *>(&a));
+                bot = __half22float2(*reinterpret_cast<const __half2 *>(&b));
+            } else {
+                top = make_float2(craw_prep(k, (uint16_t)(a & 0xffff), 0), craw_prep(k, (uint16_t)(a >> 16), 1));
+                bot = make_float2(craw_prep(k, (uint16_t)(b & 0xffff), 2), craw_prep(k, (uint16_t)(b >> 16), 3));
+            }
             *reinterpret_cast<float2 *>(&Vp[(2 * qy + 6) * VS + 2 * qx + 6]) = top;
             *reinterpret_cast<float2 *>(&Vp[(2 * qy + 7) * VS + 2 * qx + 6]) = bot;
         }

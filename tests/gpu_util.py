@@ -58,14 +58,14 @@ def cudart():
 def download_image(img: L.Image, kind: str) -> np.ndarray:
     """Copies a device image the pipeline owns to the host: kind is
     'rgba32f', 'rgba16f', 'r16', 'r32f' or 'r8'."""
-    bpp = {"rgba32f": 16, "rgba16f": 8, "r16": 2, "r32f": 4, "r8": 1}[kind]
+    bpp = {"rgba32f": 16, "rgba16f": 8, "r16": 2, "r16f": 2, "r32f": 4, "r8": 1}[kind]
     torch.cuda.synchronize()
     host = np.empty(img.pitch * img.height, np.uint8)
     ret = cudart().cudaMemcpy(host.ctypes.data, img.data, host.nbytes, 2)  # device to host
     assert ret == 0, ret
     a = host.reshape(img.height, img.pitch)[:, : img.width * bpp]
-    dt = {"rgba32f": np.float32, "rgba16f": np.float16, "r16": np.uint16, "r32f": np.float32,
-          "r8": np.uint8}[kind]
+    dt = {"rgba32f": np.float32, "rgba16f": np.float16, "r16": np.uint16, "r16f": np.float16,
+          "r32f": np.float32, "r8": np.uint8}[kind]
     a = np.ascontiguousarray(a).view(dt)
     if kind.startswith("rgba"):
         a = a.reshape(img.height, img.width, 4)

@@ -58,3 +58,22 @@ def test_cli_develop_matches_the_pipeline(tmp_path):
     assert np.array_equal(got, ref[..., :3])
     assert cli.main(["bench", "--width", str(w), "--height", str(h), "--frames", "3",
                      "--denoise", "1.0"]) == 0
+
+
+@pytest.mark.gpu
+def test_cli_highlights(tmp_path):
+    from gpu_util import develop
+
+    w, h = 128, 96
+    m = W.highlight_frame(w, h, 77)
+    m.tofile(tmp_path / "hl.raw")
+    assert cli.main(["develop", str(tmp_path / "hl.raw"), str(tmp_path / "hl.pfm"), "--width", str(w),
+                     "--height", str(h), "--space", "bt709", "--highlights"]) == 0
+    got = cli.read_pfm(tmp_path / "hl.pfm")
+    prof = W.make_profile()
+    pp = L.pipeline_params(w, h, debayer=L.DEBAYER_RCD, out_space=L.CS_BT709,
+                           flags=L.FLAG_HIGHLIGHT_RECONSTRUCTION, out_format=L.FORMAT_RGBA32F)
+    fp = L.frame_params(prof, flags=L.FRAME_HIGHLIGHT_RECONSTRUCTION)
+    with L.Context(0) as ctx, L.Pipeline(ctx, pp) as pipe:
+        ref = develop(pipe, m, fp)
+    assert np.array_equal(got, ref[..., :3])

@@ -43,11 +43,14 @@ def test_create_errors(ctx):
         with pytest.raises(L.CrawError) as e:
             L.Pipeline(ctx, L.pipeline_params(w, h, **kw))
         assert e.value.errno == 22, (w, h, kw)
-    for flag in (L.FLAG_LENS, L.FLAG_FALSE_COLOR, L.FLAG_HIGHLIGHT_RECONSTRUCTION, L.FLAG_DEFRINGE,
-                 L.FLAG_SHARPEN):
+    for flag in (L.FLAG_LENS, L.FLAG_FALSE_COLOR, L.FLAG_DEFRINGE, L.FLAG_SHARPEN):
         with pytest.raises(L.CrawError) as e:
             L.Pipeline(ctx, L.pipeline_params(64, 48, flags=flag))
         assert e.value.errno == 95
+    # The highlight reconstruction is built for the fused path only.
+    with pytest.raises(L.CrawError) as e:
+        L.Pipeline(ctx, L.pipeline_params(64, 48, flags=L.FLAG_HIGHLIGHT_RECONSTRUCTION, impl=L.IMPL_PLAIN))
+    assert e.value.errno == 95
     with pytest.raises(L.CrawError) as e:
         L.Pipeline(ctx, L.pipeline_params(64, 48, cfa=1))
     assert e.value.errno == 95
