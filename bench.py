@@ -63,8 +63,9 @@ def parse():
     ap.add_argument("--impl", default="fused", choices=["fused", "plain", "reference"])
     ap.add_argument("--storage", default="fp32", choices=["fp32", "fp16"])
     ap.add_argument("--no-extras", action="store_true", help="skip the plain/fp16/cpu side runs")
-    ap.add_argument("--extras", default="plain,fp16,batch,temporal,serve,cpu",
-                    help="comma list of side runs: plain, fp16, batch, temporal, serve, cpu")
+    ap.add_argument("--extras", default="plain,fp16,batch,temporal,serve,highlights,noise,cpu",
+                    help="comma list of side runs: plain, fp16, batch, temporal, serve, highlights, "
+                         "noise, cpu")
     ap.add_argument("--force-shape", type=int, default=-1,
                     help="denoise tile shape index instead of the autotuner's (profiling)")
     ap.add_argument("--width", type=int, default=5760)
@@ -451,6 +452,10 @@ def run_gpu(args):
             if base:
                 extras["serve"]["eq_speedup_vs_plain_fp32"] = (
                     extras["serve"]["saturated"]["eq_5760x3240_fps"] / base)
+        if "highlights" in want:
+            extras["highlights"] = run_highlights(ctx, stream)
+        if "noise" in want:
+            extras["noise_estimate"] = run_noise_estimate(cpu="cpu" in want)
 
     cpu = None
     if rank == 0 and "cpu" in want:
@@ -561,6 +566,93 @@ def run_batch_mix(ctx, stream, steps: int, warmup: int, mix=None, label: str | N
         p_.close()
     res["speedup_vs_single_frames"] = (res["fused_graph"]["frames_per_s"] /
                                        res["single_frame_pipeline"]["frames_per_s"])
+    return res
+
+
+def run_highlights(ctx, stream, nsteps: int = 20) -> dict:
+    """The headline chain (VST + NLM 1.0 + RCD + ACES AP1 + AWB) with the
+    highlight reconstruction on, at 5760x3240, on the benchmark scene and
+    on a scene whose highlights clip (2.5x under three lamps: 30 % of sites
+    near or at the clip): frames/s from CUDA events around each record and
+    the per-stage device times."""
+    import torch
+    import libcraw_gb300 as L
+    from libcraw_gb300 import workloads as W
+
+    c = W.config(2)
+    w, h = c.width, c.height
+    prof = W.make_profile()
+    fp = L.frame_params(prof, flags=L.FRAME_HIGHLIGHT_RECONSTRUCTION, **c.frame_kwargs())
+    out = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    dst = L.Image(out.data_ptr(), w * 16, L.FORMAT_RGBA32F, w, h)
+    pp = L.pipeline_params(w, h, debayer=c.debayer, out_space=c.out_space,
+                           flags=c.flags | L.FLAG_PROFILE | L.FLAG_HIGHLIGHT_RECONSTRUCTION,
+                           out_format=L.FORMAT_RGBA32F)
+    res = {"workload": f"{w}x{h}: VST + NLM 1.0 + highlight reconstruction + RCD + ACES AP1 f32 + AWB"}
+    for scene, frame in (("benchmark_scene", c.frame(0)), ("clipped_scene", W.highlight_frame(w, h, 7))):
+        t = torch.from_numpy(frame.view(np.int16)).cuda()
+        src = L.Image(t.data_ptr(), w * 2, L.FORMAT_R16_UNORM, w, h)
+        with L.Pipeline(ctx, pp) as pipe, torch.cuda.stream(stream):
+            evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+                   for _ in range(nsteps + 3)]
+            stage: dict[str, list[float]] = {}
+            for i, (e0, e1) in enumerate(evs):
+                e0.record(stream)
+                pipe.record(stream.cuda_stream, src, dst, fp)
+                e1.record(stream)
+                e1.synchronize()
+                if i >= 3:
+                    for sname, _, ms in pipe.stage_times():
+                        stage.setdefault(sname, []).append(ms)
+            torch.cuda.synchronize()
+        ms = [a.elapsed_time(b) for a, b in evs[3:]]
+        res[scene] = {"fps": 1000.0 * len(ms) / sum(ms), "ms_per_frame": statistics.mean(ms),
+                      "stage_ms": {k: statistics.mean(v) for k, v in stage.items()}}
+    return res
+
+
+def run_noise_estimate(nsteps: int = 10, cpu: bool = True) -> dict:
+    """craw_noise_estimate_cuda() on a 5760x3240 frame of the benchmark
+    scene already on the device (wall time of the call, which ends with
+    the estimate on the host), craw_noise_estimate() from host memory, and
+    the CPU oracle (the reference's algorithm restated, one host thread,
+    as the reference runs it) on the same frame."""
+    import torch
+    import libcraw_gb300 as L
+    from libcraw_gb300 import workloads as W
+
+    c = W.config(2)
+    w, h = c.width, c.height
+    prof = W.make_profile()
+    frame = c.frame(0)
+    t = torch.from_numpy(frame.view(np.int16)).cuda()
+    img = L.Image(t.data_ptr(), w * 2, L.FORMAT_R16_UNORM, w, h)
+    s = torch.cuda.Stream()
+    for _ in range(3):
+        est = L.noise_estimate_cuda(img, prof, stream=s.cuda_stream)
+    dev = []
+    for _ in range(nsteps):
+        t0 = time.perf_counter()
+        est = L.noise_estimate_cuda(img, prof, stream=s.cuda_stream)
+        dev.append(1e3 * (time.perf_counter() - t0))
+    host = []
+    for _ in range(3):
+        t0 = time.perf_counter()
+        L.noise_estimate(frame, prof)
+        host.append(1e3 * (time.perf_counter() - t0))
+    res = {"workload": f"{w}x{h} benchmark scene, default options (128 bins, 20000 samples a bin)",
+           "device_ms": statistics.median(dev), "host_frame_ms": statistics.median(host),
+           "estimate": {"a": est.model.a, "b": est.model.b, "bins": est.nb_bins,
+                        "inliers": est.nb_inliers, "fit_rms": est.fit_rms},
+           "true_model": list(W.noise_model(4.0, 40.0))}
+    if cpu:
+        sys.path.insert(0, str(ROOT / "tests"))
+        from oracle import Oracle
+        t0 = time.perf_counter()
+        ret, ref = Oracle().noise_estimate(frame, prof)
+        res["cpu_oracle_ms"] = 1e3 * (time.perf_counter() - t0)
+        res["cpu_oracle_cores"] = 1
+        res["same_as_oracle"] = ret == 0 and ref.as_tuple() == est.as_tuple()
     return res
 
 

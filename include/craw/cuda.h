@@ -70,4 +70,19 @@ typedef struct CRAWImage {
     uint32_t   width, height;
 } CRAWImage;
 
+struct CRAWProfile;
+struct CRAWNoiseEstimateParams;
+struct CRAWNoiseEstimate;
+
+/* craw_noise_estimate() (craw/noise.h) of a mosaic already on the device:
+ * an R16_UNORM image, 16-byte aligned rows. The work is enqueued on
+ * `stream` (after whatever the caller put there before), which this call
+ * then synchronises: it returns the estimate. Device scratch (about
+ * 6 bytes per sample) is allocated on the stream from the device's
+ * current memory pool and freed before returning. No reference
+ * counterpart (the reference estimates on the CPU). */
+CRAW_API int craw_noise_estimate_cuda(const CRAWImage *mosaic, const struct CRAWProfile *profile,
+                                      const struct CRAWNoiseEstimateParams *params,
+                                      struct CRAWNoiseEstimate *out, cudaStream_t stream);
+
 #endif /* CRAW_CUDA_H */

@@ -87,6 +87,20 @@ class NoiseModel(C.Structure):
     _fields_ = [("a", C.c_float), ("b", C.c_float)]
 
 
+class NoiseEstimateParams(C.Structure):
+    _fields_ = [("nb_bins", C.c_uint32), ("min_bin_samples", C.c_uint32), ("max_level", C.c_float),
+                ("padding", C.c_uint8 * 52)]
+
+
+class NoiseEstimate(C.Structure):
+    _fields_ = [("model", NoiseModel), ("nb_bins", C.c_uint32), ("nb_inliers", C.c_uint32),
+                ("fit_rms", C.c_float), ("read_noise_lsb", C.c_float), ("padding", C.c_uint8 * 40)]
+
+    def as_tuple(self):
+        return (self.model.a, self.model.b, self.nb_bins, self.nb_inliers, self.fit_rms,
+                self.read_noise_lsb)
+
+
 class Illuminant(C.Structure):
     _fields_ = [("cct", C.c_float), ("tint", C.c_float)]
 
@@ -273,6 +287,7 @@ EXPORTS = (
     "craw_server_params_init", "craw_server_stream_params_init", "craw_server_create",
     "craw_server_free", "craw_server_stream_open", "craw_server_stream_close",
     "craw_server_submit", "craw_server_poll", "craw_server_drain", "craw_server_get_stats",
+    "craw_noise_estimate_params_init", "craw_noise_estimate", "craw_noise_estimate_cuda",
 )
 
 
@@ -374,6 +389,11 @@ def lib() -> C.CDLL:
         "craw_server_poll": (i32, [vp, C.POINTER(ServerResult), u32, i32]),
         "craw_server_drain": (i32, [vp]),
         "craw_server_get_stats": (i32, [vp, C.POINTER(ServerStats)]),
+        "craw_noise_estimate_params_init": (None, [C.POINTER(NoiseEstimateParams)]),
+        "craw_noise_estimate": (i32, [vp, u32, u32, C.c_size_t, C.POINTER(Profile),
+                                      C.POINTER(NoiseEstimateParams), C.POINTER(NoiseEstimate)]),
+        "craw_noise_estimate_cuda": (i32, [C.POINTER(Image), C.POINTER(Profile), C.POINTER(NoiseEstimateParams),
+                                           C.POINTER(NoiseEstimate), vp]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -417,6 +437,38 @@ def noise_model_eval(knots: list[tuple[float, float, float]], iso: float) -> Noi
     arr = (NoiseKnot * max(1, len(knots)))(*[NoiseKnot(*k) for k in knots])
     out = NoiseModel()
     _check(lib().craw_noise_model_eval(arr, len(knots), iso, C.byref(out)), "craw_noise_model_eval")
+    return out
+
+
+def noise_estimate_params(**kw) -> NoiseEstimateParams:
+    p = NoiseEstimateParams()
+    lib().craw_noise_estimate_params_init(C.byref(p))
+    for k, v in kw.items():
+        setattr(p, k, v)
+    return p
+
+
+def noise_estimate(bayer: np.ndarray, profile: Profile,
+                   params: NoiseEstimateParams | None = None) -> NoiseEstimate:
+    """craw_noise_estimate() of an (h, w) uint16 host mosaic."""
+    bayer = np.asarray(bayer)
+    if bayer.dtype != np.uint16 or bayer.ndim != 2 or bayer.strides[1] != 2:
+        raise ValueError("an (h, w) uint16 mosaic with contiguous rows")
+    h, w = bayer.shape
+    out = NoiseEstimate()
+    _check(lib().craw_noise_estimate(bayer.ctypes.data, w, h, bayer.strides[0] // 2, C.byref(profile),
+                                     None if params is None else C.byref(params), C.byref(out)),
+           "craw_noise_estimate")
+    return out
+
+
+def noise_estimate_cuda(mosaic: Image, profile: Profile, params: NoiseEstimateParams | None = None,
+                        stream: int = 0) -> NoiseEstimate:
+    """craw_noise_estimate_cuda() of a device R16 image, on `stream`."""
+    out = NoiseEstimate()
+    _check(lib().craw_noise_estimate_cuda(C.byref(mosaic), C.byref(profile),
+                                          None if params is None else C.byref(params), C.byref(out),
+                                          stream or None), "craw_noise_estimate_cuda")
     return out
 
 

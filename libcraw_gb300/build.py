@@ -41,9 +41,10 @@ HOST_CFLAGS = ["-std=c2x", "-O2", "-fPIC", "-fvisibility=hidden", "-Wall", "-Wex
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", *ARCH, "-Xcompiler", "-fPIC",
               "-Xcompiler", "-fvisibility=hidden", f"-I{ROOT / 'include'}",
               "-diag-suppress", "177"]
-# The highlight pass decides per site whether to lift it by comparing
-# values with 0: built like the oracle, without multiply-add contraction.
-NVCC_FILE_FLAGS = {"highlight": ["-fmad=false"]}
+# The highlight pass and the noise estimator restate host code whose
+# float results they must reproduce: built like the reference's host code
+# and the oracle, without multiply-add contraction.
+NVCC_FILE_FLAGS = {"highlight": ["-fmad=false"], "noise": ["-fmad=false"]}
 
 
 def _headers(*dirs: Path) -> float:

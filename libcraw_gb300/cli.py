@@ -6,6 +6,7 @@ pipeline on frames of a given size (`cineraw --bench`, tools/cineraw.c:
     python -m libcraw_gb300.cli develop IN.raw OUT.pfm --width W --height H [options]
     python -m libcraw_gb300.cli bench --width W --height H [--frames N] [options]
     python -m libcraw_gb300.cli synth OUT.raw --width W --height H [--seed S]
+    python -m libcraw_gb300.cli noise --width W --height H [--input IN.raw] [--frames N]
 
 Options include the stages (--denoise, --temporal, --chroma strengths,
 --highlights) and, for synthetic frames, --scene highlights: the scene at
@@ -181,6 +182,34 @@ def scene(args, seed: int) -> np.ndarray:
     return W.synth_frame(args.width, args.height, seed, noise_a_dn=args.noise[0], noise_b_dn=args.noise[1])
 
 
+def cmd_noise(args) -> int:
+    """Fits the noise model of each frame (`cineraw --noise-estimate`,
+    tools/cineraw.c:2705-2730): a dump, or seeded synthetic frames, with
+    the time of each estimate."""
+    prof = camera(args)
+    params = L.noise_estimate_params()
+    if args.bins:
+        params.nb_bins = args.bins
+    if args.min_samples:
+        params.min_bin_samples = args.min_samples
+    frames = ([read_raw(args.input, args.width, args.height)] if args.input else
+              [scene(args, 4242 + i) for i in range(args.frames)])
+    for i, m in enumerate(frames):
+        t0 = time.perf_counter()
+        try:
+            est = L.noise_estimate(m, prof, params)
+        except L.CrawError as e:
+            if e.code == -61:
+                print(f"frame {i:5d}: too few levels in this frame to fit anything", file=sys.stderr)
+                return 1
+            raise
+        ms = 1e3 * (time.perf_counter() - t0)
+        print(f"frame {i:5d}: a {est.model.a:.4e} b {est.model.b:.4e}   {est.nb_bins} bins, "
+              f"{est.nb_inliers} fitted, fit error {100 * est.fit_rms:.1f}%, read noise "
+              f"{est.read_noise_lsb:.2f} code values  ({ms:.2f} ms)")
+    return 0
+
+
 def cmd_synth(args) -> int:
     scene(args, args.seed).astype(np.uint16).tofile(args.output)
     return 0
@@ -229,6 +258,13 @@ def parser() -> argparse.ArgumentParser:
     p.add_argument("--seed", type=int, default=1)
     common(p, need_io=False)
     p.set_defaults(fn=cmd_synth)
+    p = sub.add_parser("noise", help="fit the sensor noise model of frames (on the GPU)")
+    p.add_argument("--input", default=None, help="a mosaic dump (default: synthetic frames)")
+    p.add_argument("--frames", type=int, default=3, help="synthetic frames to fit")
+    p.add_argument("--bins", type=int, default=0, help="intensity bins (0: 128)")
+    p.add_argument("--min-samples", type=int, default=0, help="samples a bin needs (0: 20000)")
+    common(p)
+    p.set_defaults(fn=cmd_noise)
     return ap
 
 

@@ -173,6 +173,44 @@ int64_t craw_k_highlight_levels(int32_t width, int32_t height, CRAWKHighlight *k
 
 int craw_k_highlights(const CRAWKHighlight *k, const CRAWKHighlightIO *io, cudaStream_t s);
 
+/* ------------------------------------------------- noise-model estimation */
+
+/* The device half of craw_noise_estimate(): every interior sample of the
+ * four CFA planes gets its |3x3 high-pass| and a bin by its 9x9 plane
+ * mean; each bin's count, the exact sum of its means and its median
+ * |high-pass| come back in CRAWKNoiseBin. The host fits the line. */
+typedef struct CRAWKNoise {
+    int32_t width, height;       /* mosaic, both even */
+    float black[4], white[4];    /* profile levels per quad site */
+    int32_t nb_bins;
+    float max_level;
+} CRAWKNoise;
+
+typedef struct CRAWKNoiseBin {
+    uint32_t count;       /* samples in the bin */
+    uint32_t median;      /* bits of the (count / 2)-th smallest |high-pass| */
+    /* The sum of the bin's means x 2^64: each mean as a 96-bit integer
+     * (exact for means >= 2^-40, up to 2^31), its three 32-bit words
+     * summed separately: sum = sum[2] 2^64 + sum[1] 2^32 + sum[0]. */
+    uint64_t sum[3];
+} CRAWKNoiseBin;
+
+/* Device scratch craw_k_noise_bins needs, in bytes. */
+size_t craw_k_noise_scratch(int32_t width, int32_t height, int32_t nb_bins);
+
+/* Fills bins[0 .. nb_bins) (device memory) on stream s. */
+int craw_k_noise_bins(const CRAWKNoise *k, const uint16_t *src, size_t src_pitch, void *scratch,
+                      CRAWKNoiseBin *bins, cudaStream_t s);
+
+/* The least-trimmed-squares cost of the line through every pair of bins
+ * i < j (the sum of the `keep` smallest squared log residuals, added in
+ * ascending order): cost[i * nb + j], +inf where the pair gives no
+ * physical line. m, v: the bins' mean level and variance; lv = ln v,
+ * computed on the host. All device arrays; nb <= CRAW_K_NOISE_MAX_BINS. */
+#define CRAW_K_NOISE_MAX_BINS 512
+int craw_k_noise_lts(const double *m, const double *v, const double *lv, int32_t nb, int32_t keep,
+                     double *cost, cudaStream_t s);
+
 /* ------------------------------------------------------------- batch */
 
 /* One frame of a batch: its constants and buffers, how many tiles each

@@ -210,58 +210,6 @@ struct Search {
     }
 };
 
-/* Two fp32 lanes in one 64-bit register, for the sm_100 family's packed
- * f32x2 add / sub / mul / fma (one instruction for both columns of a
- * thread, the same IEEE rounding per lane as the scalar forms). */
-typedef unsigned long long f2x;
-
-CRAW_DEV f2x f2_pack(float lo, float hi)
-{
-    f2x r;
-    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-    return r;
-}
-CRAW_DEV float f2_lo(f2x a)
-{
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a));
-    return lo;
-}
-CRAW_DEV float f2_hi(f2x a)
-{
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a));
-    return hi;
-}
-CRAW_DEV f2x f2_add(f2x a, f2x b)
-{
-    f2x d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-CRAW_DEV f2x f2_sub(f2x a, f2x b)
-{
-    f2x d;
-    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-CRAW_DEV f2x f2_mul(f2x a, f2x b)
-{
-    f2x d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-    return d;
-}
-CRAW_DEV f2x f2_fma(f2x a, f2x b, f2x c)
-{
-    f2x d;
-    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
-    return d;
-}
-CRAW_DEV f2x f2_ld(const float *p)   /* p 8-byte aligned */
-{
-    return *reinterpret_cast<const f2x *>(p);
-}
-
 /* The search of a thread's 2 columns x M rows with the two columns in one
  * packed register: squared differences, the column sums of the patch, the
  * weight's affine steps, the weight sum and the weighted sum are f32x2

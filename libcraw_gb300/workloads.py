@@ -209,3 +209,17 @@ def highlight_frame(width: int, height: int, seed: int, gain: float = 2.5,
         d = np.hypot(xx - cx, yy - cy)
         v += np.clip(1.0 - d / r, 0.0, 1.0) * RANGE_DN * rng.uniform(1.0, 3.0)
     return np.clip(np.rint(v + BLACK_DN), 0, WHITE_DN).astype(np.uint16)
+
+
+def noise_ramp(width: int, height: int, seed: int, a_dn: float = 4.0, b_dn: float = 40.0,
+               lo: float = 0.01, hi: float = 0.95) -> np.ndarray:
+    """A mosaic whose signal is a horizontal ramp from `lo` to `hi` of the
+    range above black, the same on every site, with Poisson-Gaussian noise
+    of variance a_dn * signal + b_dn (12-bit DN), rounded and clipped: a
+    frame whose every bin holds nothing but noise (a ramp is locally
+    linear, which the estimator's high-pass removes), so the noise-model
+    estimate should recover (a_dn, b_dn) / (range, range^2)."""
+    rng = np.random.default_rng(seed)
+    sig = np.broadcast_to(np.linspace(lo, hi, width) * RANGE_DN, (height, width))
+    v = BLACK_DN + sig + rng.standard_normal((height, width)) * np.sqrt(a_dn * sig + b_dn)
+    return np.clip(np.rint(v), 0, 65535).astype(np.uint16)

@@ -330,6 +330,278 @@ ORC_API int orc_noise_model(const CRAWFrameParams *fp, CRAWNoiseModel *out)
     return orc_noise_model_eval(p->noise_knots, p->nb_noise_knots, iso, out);
 }
 
+/* ------------------------------------------------ noise-model estimation */
+
+/* Constants of reference lib/noise.c:14-27 and 145: the MAD of a unit
+ * Gaussian, the Tukey cut, the floor on the residual scale, the radius of
+ * the box mean. */
+#define ORC_NE_MAD 0.674489750196081746f
+#define ORC_NE_TUKEY 4.685
+#define ORC_NE_FLOOR 0.02
+#define ORC_NE_R 4
+
+static int orc_cmp_f(const void *a, const void *b)
+{
+    float x = *(const float *)a, y = *(const float *)b;
+    return (x > y) - (x < y);
+}
+
+static int orc_cmp_d(const void *a, const void *b)
+{
+    double x = *(const double *)a, y = *(const double *)b;
+    return (x > y) - (x < y);
+}
+
+/* Sum of the `keep` smallest of v[0..n) (sorted in place, ascending). */
+static double orc_ne_trimmed(double *v, int n, int keep)
+{
+    double s = 0.0;
+    qsort(v, (size_t)n, sizeof(*v), orc_cmp_d);
+    for (int k = 0; k < keep; k++)
+        s += v[k];
+    return s;
+}
+
+/* Median |x| of x[0..n) times 1.4826 (the Gaussian sigma), floored. */
+static double orc_ne_scale(const double *x, int n, double *work)
+{
+    double s;
+    for (int k = 0; k < n; k++)
+        work[k] = fabs(x[k]);
+    qsort(work, (size_t)n, sizeof(*work), orc_cmp_d);
+    s = 1.4826 * work[n / 2];
+    return s < ORC_NE_FLOOR ? ORC_NE_FLOOR : s;
+}
+
+/* Estimate of var = a u + b from one RGGB frame: reference
+ * lib/noise.c:338-504 (binning 396-450, bin statistics 452-467), the
+ * least-trimmed-squares seed 187-250 and the reweighted Gauss-Newton
+ * 252-336. Bin sums follow the reference's sample order (plane, row,
+ * column) so that the bin means are its doubles bit for bit. */
+ORC_API int orc_noise_estimate(const uint16_t *bayer, uint32_t width, uint32_t height,
+                               size_t stride, const CRAWProfile *pr,
+                               const CRAWNoiseEstimateParams *params, CRAWNoiseEstimate *out)
+{
+    uint32_t nbins, min_n;
+    float maxl;
+    int w2, h2, ret = 0, nb = 0, nin = 0;
+    float *plane = NULL, *res = NULL;
+    uint16_t *lab = NULL;
+    size_t *cnt = NULL, *start = NULL, ns = 0;
+    double *msum = NULL, *m = NULL, *v = NULL, *c = NULL, *work = NULL, *rr = NULL;
+    double a = 0.0, b = 0.0, best = INFINITY, scale, la, lb, rms = 0.0, range0;
+
+    if (!bayer || !pr || !out)
+        return -EINVAL;
+    if (pr->cfa != CRAW_CFA_RGGB)
+        return -ENOTSUP;
+    if ((width & 1) || (height & 1) || width < 32 || height < 32 || stride < width)
+        return -EINVAL;
+    nbins = params && params->nb_bins ? params->nb_bins : 128;
+    min_n = params && params->min_bin_samples ? params->min_bin_samples : 20000;
+    maxl = params && params->max_level > 0.0f ? params->max_level : 0.98f;
+    if (nbins < 8 || nbins > CRAW_NOISE_MAX_BINS)
+        return -EINVAL;
+    for (int s = 0; s < 4; s++)
+        if (!(pr->white_level[s] > pr->black_level[s]))
+            return -EINVAL;
+    w2 = (int)width / 2;
+    h2 = (int)height / 2;
+    if (w2 < 2 * ORC_NE_R + 1 || h2 < 2 * ORC_NE_R + 1)
+        return -EINVAL;
+
+    ns = (size_t)4 * (size_t)(w2 - 2 * ORC_NE_R) * (size_t)(h2 - 2 * ORC_NE_R);
+    plane = malloc((size_t)w2 * h2 * sizeof(*plane));
+    res = malloc(ns * sizeof(*res));
+    lab = malloc(ns * sizeof(*lab));
+    cnt = calloc(nbins, sizeof(*cnt));
+    start = calloc(nbins + 1, sizeof(*start));
+    msum = calloc(nbins, sizeof(*msum));
+    m = malloc(nbins * sizeof(*m));
+    v = malloc(nbins * sizeof(*v));
+    c = malloc(nbins * sizeof(*c));
+    work = malloc(nbins * sizeof(*work));
+    rr = malloc(nbins * sizeof(*rr));
+    if (!plane || !res || !lab || !cnt || !start || !msum || !m || !v || !c || !work || !rr) {
+        ret = -ENOMEM;
+        goto done;
+    }
+
+    /* Every interior sample of every plane: its |high-pass| and its bin
+     * (0xffff: not binned). */
+    ns = 0;
+    for (int s = 0; s < 4; s++) {
+        const int px = s & 1, py = s >> 1;
+        const double black = pr->black_level[s];
+        const double range = pr->white_level[s] - pr->black_level[s];
+        for (int k = 0; k < h2; k++)
+            for (int i = 0; i < w2; i++) {
+                const double raw = bayer[(size_t)(2 * k + py) * stride + 2 * i + px] * (1.0 / 65535.0);
+                plane[(size_t)k * w2 + i] = (float)((raw - black) / range);
+            }
+        for (int k = ORC_NE_R; k < h2 - ORC_NE_R; k++)
+            for (int i = ORC_NE_R; i < w2 - ORC_NE_R; i++, ns++) {
+                const float *p = plane + (size_t)k * w2 + i;
+                float hp, mean = 0.0f;
+                int bi;
+                hp = (p[-w2 - 1] + p[-w2 + 1] + p[w2 - 1] + p[w2 + 1] -
+                      2.0f * (p[-w2] + p[w2] + p[-1] + p[1]) + 4.0f * p[0]) * (1.0f / 6.0f);
+                for (int dy = -ORC_NE_R; dy <= ORC_NE_R; dy++)
+                    for (int dx = -ORC_NE_R; dx <= ORC_NE_R; dx++)
+                        mean += p[dy * w2 + dx];
+                mean *= 1.0f / 81;
+                lab[ns] = 0xffff;
+                if (!(mean > 0.0f) || mean > maxl)
+                    continue;
+                bi = (int)(sqrtf(mean) * (float)nbins);
+                bi = bi < 0 ? 0 : (bi > (int)nbins - 1 ? (int)nbins - 1 : bi);
+                lab[ns] = (uint16_t)bi;
+                res[ns] = fabsf(hp);
+                cnt[bi]++;
+                msum[bi] += mean;
+            }
+    }
+
+    /* Group the residuals by bin (counting sort), then each bin's median. */
+    for (uint32_t i = 0; i < nbins; i++)
+        start[i + 1] = start[i] + cnt[i];
+    {
+        float *grp = malloc((start[nbins] ? start[nbins] : 1) * sizeof(*grp));
+        size_t *fill = calloc(nbins, sizeof(*fill));
+        if (!grp || !fill) {
+            free(grp);
+            free(fill);
+            ret = -ENOMEM;
+            goto done;
+        }
+        for (size_t j = 0; j < ns; j++)
+            if (lab[j] != 0xffff)
+                grp[start[lab[j]] + fill[lab[j]]++] = res[j];
+        for (uint32_t i = 0; i < nbins; i++) {
+            double sigma;
+            if (cnt[i] < min_n)
+                continue;
+            qsort(grp + start[i], cnt[i], sizeof(*grp), orc_cmp_f);
+            sigma = grp[start[i] + cnt[i] / 2] / ORC_NE_MAD;
+            if (!(sigma > 0.0))
+                continue;
+            m[nb] = msum[i] / (double)cnt[i];
+            v[nb] = sigma * sigma;
+            c[nb] = (double)cnt[i];
+            nb++;
+        }
+        free(grp);
+        free(fill);
+    }
+    if (nb < 3) {
+        ret = -ENODATA;
+        goto done;
+    }
+
+    /* Seed: the physical line through two bins whose two-thirds smallest
+     * squared log residuals sum least (first found on a tie). */
+    {
+        const int keep = nb * 2 / 3 + 1;
+        for (int i = 0; i < nb; i++)
+            for (int j = i + 1; j < nb; j++) {
+                double sa, sb, cost;
+                if (m[j] - m[i] < 1e-5)
+                    continue;
+                sa = (v[j] - v[i]) / (m[j] - m[i]);
+                sb = v[i] - sa * m[i];
+                if (!(sa > 0.0) || sb < 0.0)
+                    continue;
+                for (int k = 0; k < nb; k++) {
+                    const double d = log(v[k]) - log(sa * m[k] + sb);
+                    work[k] = d * d;
+                }
+                cost = orc_ne_trimmed(work, nb, keep);
+                if (cost < best) {
+                    best = cost;
+                    a = sa;
+                    b = sb;
+                }
+            }
+        if (!(a > 0.0)) {
+            ret = -ENODATA;
+            goto done;
+        }
+        scale = sqrt(best / keep);
+    }
+
+    /* Refinement in (ln a, ln b): 40 damped Gauss-Newton steps at most,
+     * Tukey weights times ln(1 + count), the scale re-measured every 8. */
+    la = log(a);
+    lb = log(b > 1e-16 ? b : 1e-16);
+    if (scale < ORC_NE_FLOOR)
+        scale = ORC_NE_FLOOR;
+    for (int it = 0; it < 40; it++) {
+        const double ea = exp(la), eb = exp(lb);
+        double saa = 0.0, sab = 0.0, sbb = 0.0, ra = 0.0, rb = 0.0, det, d0, d1, cut;
+        for (int k = 0; k < nb; k++)
+            rr[k] = log(v[k]) - log(ea * m[k] + eb);
+        if ((it & 7) == 0)
+            scale = orc_ne_scale(rr, nb, work);
+        cut = ORC_NE_TUKEY * scale;
+        for (int k = 0; k < nb; k++) {
+            const double den = ea * m[k] + eb, ja = ea * m[k] / den, jb = eb / den;
+            const double u = rr[k] / cut;
+            double w = fabs(u) < 1.0 ? (1.0 - u * u) * (1.0 - u * u) : 0.0;
+            w *= log(1.0 + c[k]);
+            saa += w * ja * ja;
+            sab += w * ja * jb;
+            sbb += w * jb * jb;
+            ra += w * ja * rr[k];
+            rb += w * jb * rr[k];
+        }
+        det = (saa + 1e-9) * (sbb + 1e-9) - sab * sab;
+        if (!(fabs(det) > 1e-30))
+            break;
+        d0 = ((sbb + 1e-9) * ra - sab * rb) / det;
+        d1 = (-sab * ra + (saa + 1e-9) * rb) / det;
+        d0 = d0 < -0.5 ? -0.5 : (d0 > 0.5 ? 0.5 : d0);
+        d1 = d1 < -0.5 ? -0.5 : (d1 > 0.5 ? 0.5 : d1);
+        la += d0;
+        lb += d1;
+        if (lb < -40.0)
+            lb = -40.0;
+        if (fabs(d0) < 1e-9 && fabs(d1) < 1e-9)
+            break;
+    }
+    a = exp(la);
+    b = lb <= -40.0 ? 0.0 : exp(lb);
+
+    for (int k = 0; k < nb; k++) {
+        const double d = log(v[k]) - log(a * m[k] + b);
+        if (fabs(d) < 0.35) {
+            rms += d * d;
+            nin++;
+        }
+    }
+    rms = sqrt(rms / (nin ? nin : 1));
+    range0 = pr->white_level[0] - pr->black_level[0];
+    memset(out, 0, sizeof(*out));
+    out->model.a = (float)a;
+    out->model.b = (float)b;
+    out->nb_bins = (uint32_t)nb;
+    out->nb_inliers = (uint32_t)nin;
+    out->fit_rms = (float)rms;
+    out->read_noise_lsb = (float)(sqrt(b) * range0 * 65535.0);
+done:
+    free(plane);
+    free(res);
+    free(lab);
+    free(cnt);
+    free(start);
+    free(msum);
+    free(m);
+    free(v);
+    free(c);
+    free(work);
+    free(rr);
+    return ret;
+}
+
 /* AWB histogram of 8x8 block means, reference lib/awb.c:213-296. */
 ORC_API int orc_awb_histogram(const float *rgb, uint32_t width, uint32_t height, size_t stride,
                               int channels, const float wb[3], uint32_t *count,

@@ -26,6 +26,9 @@ int orc_colorspace_from_xyz_f(int cs, float o[3][3]);
 void orc_gamut_params(struct orc_gamut *g);
 int orc_noise_model_eval(const CRAWNoiseKnot *k, uint32_t n, float iso, CRAWNoiseModel *out);
 int orc_noise_model(const CRAWFrameParams *fp, CRAWNoiseModel *out);
+int orc_noise_estimate(const uint16_t *bayer, uint32_t width, uint32_t height, size_t stride,
+                       const CRAWProfile *profile, const CRAWNoiseEstimateParams *params,
+                       CRAWNoiseEstimate *out);
 int orc_awb_histogram(const float *rgb, uint32_t width, uint32_t height, size_t stride,
                       int channels, const float wb[3], uint32_t *count,
                       uint32_t *weight, uint32_t *weight_bright);

@@ -179,6 +179,13 @@ def main() -> None:
         out[f"awb_smooth/{name}"] = AC.run_smoother(ref.lib, params, seed_il, ev)
     out["locus/rows"] = AC.run_locus(ref.lib, prof)
 
+    # Noise-model estimation (reference lib/noise.c:338-504).
+    import noise_cases as NC
+    for name, m, params in NC.cases():
+        ret, est = ref.noise_estimate(m, prof, params)
+        out[f"noise_est/{name}/in"] = m
+        out[f"noise_est/{name}/out"] = NC.row(ret, est)
+
     np.savez_compressed(HERE / "reference_outputs.npz", **out)
     print(f"wrote {HERE / 'reference_outputs.npz'} ({len(out)} arrays)")
 

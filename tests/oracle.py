@@ -33,6 +33,15 @@ def _sig(lib, name, res, args):
     return fn
 
 
+def _noise_estimate(fn, bayer, profile, params):
+    bayer = np.ascontiguousarray(bayer, np.uint16)
+    h, w = bayer.shape
+    out = L.NoiseEstimate()
+    ret = fn(bayer.ctypes.data, w, h, w, C.byref(profile), None if params is None else C.byref(params),
+             C.byref(out))
+    return ret, out
+
+
 class Oracle:
     """The restatement (float: ``f32``, double: ``f64``)."""
 
@@ -53,7 +62,13 @@ class Oracle:
         _sig(lib, "orc_colorspace_from_xyz_f", i32, [i32, P(C.c_float * 9)])
         _sig(lib, "orc_gamut_params", None, [P(GamutParams)])
         _sig(lib, "orc_noise_model_eval", i32, [P(L.NoiseKnot), u32, f32, P(L.NoiseModel)])
+        _sig(lib, "orc_noise_estimate", i32, [vp, u32, u32, sz, P(L.Profile), P(L.NoiseEstimateParams),
+                                              P(L.NoiseEstimate)])
         self.prefix = "orc_"
+
+    def noise_estimate(self, bayer, profile, params=None):
+        """(return code, estimate) of the restated craw_noise_estimate."""
+        return _noise_estimate(self.lib.orc_noise_estimate, bayer, profile, params)
 
     def _dt(self, s):
         return np.float32 if s == "f32" else np.float64
@@ -187,6 +202,11 @@ class Reference:
         h, w, _ = out.shape
         assert self.lib.craw_ref_color(out.ctypes.data, w, h, C.byref(fp), out_space) == 0
         return out
+
+    def noise_estimate(self, bayer, profile, params=None):
+        _sig(self.lib, "craw_noise_estimate", i32, [vp, u32, u32, sz, P(L.Profile), P(L.NoiseEstimateParams),
+                                                    P(L.NoiseEstimate)])
+        return _noise_estimate(self.lib.craw_noise_estimate, bayer, profile, params)
 
     def awb_histogram(self, rgba, wb):
         rgba = np.ascontiguousarray(rgba, np.float32)

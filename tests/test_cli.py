@@ -34,7 +34,7 @@ def test_help_lists_commands(capsys):
     with pytest.raises(SystemExit):
         cli.main(["--help"])
     out = capsys.readouterr().out
-    for c in ("develop", "bench", "synth"):
+    for c in ("develop", "bench", "synth", "noise"):
         assert c in out
 
 
@@ -77,3 +77,15 @@ def test_cli_highlights(tmp_path):
     with L.Context(0) as ctx, L.Pipeline(ctx, pp) as pipe:
         ref = develop(pipe, m, fp)
     assert np.array_equal(got, ref[..., :3])
+
+
+@pytest.mark.gpu
+def test_cli_noise(tmp_path, capsys):
+    w, h = 1024, 768
+    m = W.noise_ramp(w, h, 88, lo=0.0)
+    m.tofile(tmp_path / "n.raw")
+    assert cli.main(["noise", "--input", str(tmp_path / "n.raw"), "--width", str(w), "--height", str(h),
+                     "--bins", "64", "--min-samples", "1000"]) == 0
+    line = capsys.readouterr().out.strip().splitlines()[-1]
+    est = L.noise_estimate(m, W.make_profile(), L.noise_estimate_params(nb_bins=64, min_bin_samples=1000))
+    assert f"a {est.model.a:.4e} b {est.model.b:.4e}" in line and f"{est.nb_bins} bins" in line
