@@ -269,6 +269,7 @@ for _s, _n in ((Profile, 1264), (FrameParams, 264), (PipelineParams, 256), (Cuda
 EXPORTS = (
     "craw_version_int", "craw_log", "craw_context_create", "craw_context_free",
     "craw_cuda_check_device", "craw_debug_fail_alloc", "craw_debug_force_denoise_shape",
+    "craw_debug_rcd_tma", "craw_debug_kernel_errors",
     "craw_pipeline_params_init", "craw_frame_params_init", "craw_pipeline_create",
     "craw_pipeline_free", "craw_pipeline_record", "craw_pipeline_get_awb_histogram",
     "craw_pipeline_get_awb_histogram_n", "craw_pipeline_get_stage_times",
@@ -348,6 +349,8 @@ def lib() -> C.CDLL:
         "craw_cuda_check_device": (i32, [i32, C.POINTER(C.c_char_p)]),
         "craw_debug_fail_alloc": (None, [i32]),
         "craw_debug_force_denoise_shape": (i32, [i32]),
+        "craw_debug_rcd_tma": (i32, [i32]),
+        "craw_debug_kernel_errors": (i32, [vp]),
         "craw_pipeline_params_init": (None, [C.POINTER(PipelineParams)]),
         "craw_frame_params_init": (None, [C.POINTER(FrameParams)]),
         "craw_pipeline_create": (i32, [vp, C.POINTER(PipelineParams), C.POINTER(vp)]),
@@ -626,6 +629,11 @@ class Pipeline:
                "craw_pipeline_get_kernel_config")
         return a.value, b.value
 
+    def kernel_errors(self) -> int:
+        """Waits for the device and returns (and clears) the error bits the
+        pipeline's kernels set: 0 when all is well."""
+        return _check(lib().craw_debug_kernel_errors(self._h), "craw_debug_kernel_errors")
+
     def temporal_state(self) -> tuple[Image, Image]:
         lvl, var = Image(), Image()
         _check(lib().craw_pipeline_get_temporal_state(self._h, C.byref(lvl), C.byref(var)),
@@ -837,3 +845,9 @@ def debug_force_denoise_shape(shape: int) -> None:
     """Every pipeline created from now uses denoise shape `shape` (-1: the
     autotuner's)."""
     _check(lib().craw_debug_force_denoise_shape(shape), "craw_debug_force_denoise_shape")
+
+
+def debug_rcd_tma(on: bool) -> bool:
+    """RCD interior tiles by one TMA tile copy (True, the default) or by
+    plain loads; returns the previous setting."""
+    return bool(lib().craw_debug_rcd_tma(1 if on else 0))

@@ -170,6 +170,13 @@ CRAW_API void craw_debug_fail_alloc(int k)
     craw_fail_countdown = k;
 }
 
+CRAW_API int craw_debug_rcd_tma(int on)
+{
+    const int was = craw_k_rcd_tma;
+    craw_k_rcd_tma = on ? 1 : 0;
+    return was;
+}
+
 int craw_dev_alloc(CRAWContext *ctx, void **ptr, size_t bytes)
 {
     *ptr = NULL;

@@ -86,6 +86,7 @@ struct CRAWPipeline {
     uint64_t *awb_rec;
     uint8_t *awb_dev;         /* HIST_BYTES + DEFER_BYTES + 4, mirrors a slot */
     uint32_t nb_blocks;
+    uint32_t *kerr;           /* CRAW_K_ERR_* bits the kernels set */
 
     /* Plain-pipeline scratch. */
     float *p_v, *p_scratch, *p_t, *p_var;
@@ -135,7 +136,7 @@ static void release(CRAWPipeline *p)
     CRAWContext *ctx = p->ctx;
     void *bufs[] = {
         p->clean, p->lvl[0], p->lvl[1], p->var[0], p->var[1], p->inter, p->q, p->qf,
-        p->awb_rec, p->awb_dev, p->p_v, p->p_scratch, p->p_t, p->p_var,
+        p->awb_rec, p->awb_dev, p->kerr, p->p_v, p->p_scratch, p->p_t, p->p_var,
         p->hl_mosaic, p->hl_levels,
     };
     cudaSetDevice(ctx->device);
@@ -156,15 +157,32 @@ static void release(CRAWPipeline *p)
 /* The autotuner: the fastest denoise tile shape for this frame size, with
  * and without a temporal history, timed on the context's own stream over a
  * scratch mosaic (the filter's work does not depend on the data), and
- * remembered for the process so that a second pipeline of the same size
- * starts at once. */
+ * remembered for the process (each of the two on its own) so that every
+ * later pipeline of the same size starts at once with the same shapes:
+ * pipelines of one size give the same results. */
 #define TUNE_CACHE 32
 static struct tune_entry {
     uint32_t w, h;
     int shape[2];
+    bool known[2];
 } tune_cache[TUNE_CACHE];
 static int tune_nb;
 static pthread_mutex_t tune_lock = PTHREAD_MUTEX_INITIALIZER;
+
+/* The cache entry of a size, created if there is room; NULL otherwise.
+ * Called with tune_lock held. */
+static struct tune_entry *tune_entry(uint32_t w, uint32_t h, bool create)
+{
+    for (int i = 0; i < tune_nb; i++)
+        if (tune_cache[i].w == w && tune_cache[i].h == h)
+            return &tune_cache[i];
+    if (!create || tune_nb == TUNE_CACHE)
+        return NULL;
+    memset(&tune_cache[tune_nb], 0, sizeof(tune_cache[0]));
+    tune_cache[tune_nb].w = w;
+    tune_cache[tune_nb].h = h;
+    return &tune_cache[tune_nb++];
+}
 
 static int time_denoise(CRAWPipeline *p, const CRAWKDenoise *k, const CRAWKDenoiseIO *io, int shape,
                         float *ms)
@@ -203,17 +221,19 @@ static int autotune(CRAWPipeline *p)
     uint8_t *var = NULL;
     size_t mp, lp, vp;
     int ret = 0;
+    bool need[2] = { p->has_denoise, p->has_temporal };
+    struct tune_entry *e;
 
     pthread_mutex_lock(&tune_lock);
-    for (int i = 0; i < tune_nb; i++) {
-        if (tune_cache[i].w == w && tune_cache[i].h == h) {
-            p->dn_shape[0] = tune_cache[i].shape[0];
-            p->dn_shape[1] = tune_cache[i].shape[1];
-            pthread_mutex_unlock(&tune_lock);
-            return 0;
-        }
-    }
+    if ((e = tune_entry(w, h, false)))
+        for (int hist = 0; hist < 2; hist++)
+            if (need[hist] && e->known[hist]) {
+                p->dn_shape[hist] = e->shape[hist];
+                need[hist] = false;
+            }
     pthread_mutex_unlock(&tune_lock);
+    if (!need[0] && !need[1])
+        return 0;
 
     if ((ret = alloc_pitched(p, (void **)&mosaic, &mp, (size_t)w * 2, h)) < 0 ||
         (ret = alloc_pitched(p, (void **)&lvl, &lp, (size_t)w * 4, h)) < 0 ||
@@ -242,9 +262,7 @@ static int autotune(CRAWPipeline *p)
             k.black[s4] = 0.0f; k.inv_range[s4] = 16.0f; k.range[s4] = 0.0625f;
         }
         k.mode = CRAW_K_DN_SPATIAL | (hist ? CRAW_K_DN_TEMPORAL | CRAW_K_DN_HISTORY : 0);
-        if (!hist && !p->has_denoise)
-            continue;
-        if (hist && !p->has_temporal)
+        if (!need[hist])
             continue;
         for (int shape = 0; shape < CRAW_K_DN_SHAPE_NB; shape++) {
             float ms;
@@ -258,14 +276,20 @@ static int autotune(CRAWPipeline *p)
         craw_log(ctx, CRAW_LOG_VERBOSE, "autotune %ux%u %s: denoise shape %d, %.3f ms\n", w, h,
                  hist ? "temporal" : "spatial", p->dn_shape[hist], (double)best);
     }
+    /* Another thread may have tuned the same size meanwhile: its shapes
+     * win, so that every pipeline of the size agrees. */
     pthread_mutex_lock(&tune_lock);
-    if (tune_nb < TUNE_CACHE && p->has_denoise && p->has_temporal) {
-        tune_cache[tune_nb].w = w;
-        tune_cache[tune_nb].h = h;
-        tune_cache[tune_nb].shape[0] = p->dn_shape[0];
-        tune_cache[tune_nb].shape[1] = p->dn_shape[1];
-        tune_nb++;
-    }
+    if ((e = tune_entry(w, h, true)))
+        for (int hist = 0; hist < 2; hist++) {
+            if (!need[hist])
+                continue;
+            if (e->known[hist]) {
+                p->dn_shape[hist] = e->shape[hist];
+            } else {
+                e->shape[hist] = p->dn_shape[hist];
+                e->known[hist] = true;
+            }
+        }
     pthread_mutex_unlock(&tune_lock);
 done:
     craw_dev_free(ctx, mosaic);
@@ -286,6 +310,19 @@ CRAW_API int craw_pipeline_get_kernel_config(CRAWPipeline *p, int *denoise_shape
     if (denoise_shape_history)
         *denoise_shape_history = p->dn_shape[1];
     return 0;
+}
+
+CRAW_API int craw_debug_kernel_errors(CRAWPipeline *p)
+{
+    uint32_t bits = 0;
+    if (!p || !p->kerr)
+        return CRAW_ERROR(EINVAL);
+    cudaSetDevice(p->ctx->device);
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(&bits, p->kerr, sizeof(bits), cudaMemcpyDeviceToHost) != cudaSuccess ||
+        cudaMemset(p->kerr, 0, sizeof(bits)) != cudaSuccess)
+        return CRAW_ERROR(EIO);
+    return (int)bits;
 }
 
 CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *params,
@@ -426,6 +463,12 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
             }
             memset(p->slots[i].host, 0, HIST_BYTES + DEFER_BYTES + 16);
         }
+    }
+    if ((ret = craw_dev_alloc(ctx, (void **)&p->kerr, 16)) < 0)
+        goto fail;
+    if (cudaMemsetAsync(p->kerr, 0, 16, ctx->stream) != cudaSuccess) {
+        ret = CRAW_ERROR(EIO);
+        goto fail;
     }
     if (p->plain) {
         size_t n = (size_t)w * h;
@@ -611,6 +654,7 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
     dio.src = mosaic;
     dio.src_pitch = mosaic_pitch;
     dio.awb = awb;
+    dio.err = p->kerr;
 
     /* Highlight reconstruction (reference pipeline.c:2047-2062): the
      * rebuilt, balanced fp16 mosaic replaces the one the debayer reads, and

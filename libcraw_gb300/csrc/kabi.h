@@ -110,12 +110,22 @@ typedef struct CRAWKDevelopIO {
     void *inter; size_t inter_pitch;                    /* NULL: not kept */
     void *quarter; size_t quarter_pitch;                /* chroma: block means out */
     CRAWKAwbOut awb;
+    uint32_t *err;                                      /* device word a kernel ORs
+                                                         * CRAW_K_ERR_* into; NULL: none */
 } CRAWKDevelopIO;
+
+/* Kernel error bits: a wait on a TMA copy that did not complete within
+ * its bound (the tile is skipped). */
+#define CRAW_K_ERR_TMA_WAIT 1u
 
 /* Prep + debayer + (colour to dst | chroma block means) + AWB records +
  * optional intermediate, in one kernel. */
 int craw_k_develop(const CRAWKDevelop *k, const CRAWKDevelopIO *io, int shape,
                    cudaStream_t s);
+
+/* 1 (default): the RCD's interior tiles bring their mosaic in with one TMA
+ * tile copy; 0: with plain loads (craw_debug_rcd_tma). */
+extern int craw_k_rcd_tma;
 
 /* ------------------------------------------------------------- chroma */
 

@@ -58,12 +58,14 @@ CRAW_DEV float f2_lo(f2x a)
 {
     float lo, hi;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a));
+    (void)hi;
     return lo;
 }
 CRAW_DEV float f2_hi(f2x a)
 {
     float lo, hi;
     asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a));
+    (void)lo;
     return hi;
 }
 CRAW_DEV f2x f2_add(f2x a, f2x b)

@@ -333,6 +333,22 @@ struct RcdQuads {
     CRAW_DEV float2 &G(int qx, int qy) const { return Gq[(qy + 1) * GS + qx + 1]; }
     CRAW_DEV float2 &Cat(int qx, int qy) const { return Cq[(qy + 1) * GS + qx + 1]; }
 
+    /* Quad (qx, qy) of the tile prepped into V from its two rows of
+     * samples (a: R, Gr; b: Gb, B; 16 bits each). */
+    CRAW_DEV void put_quad(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int qx, int qy, uint32_t a, uint32_t b)
+    {
+        float2 top, bot;
+        if (io.src_f16) {   /* rebuilt highlights: fp16, already prepped */
+            top = __half22float2(*reinterpret_cast<const __half2 *>(&a));
+            bot = __half22float2(*reinterpret_cast<const __half2 *>(&b));
+        } else {
+            top = make_float2(craw_prep(k, (uint16_t)(a & 0xffff), 0), craw_prep(k, (uint16_t)(a >> 16), 1));
+            bot = make_float2(craw_prep(k, (uint16_t)(b & 0xffff), 2), craw_prep(k, (uint16_t)(b >> 16), 3));
+        }
+        *reinterpret_cast<float2 *>(&Vp[(2 * qy + 6) * VS + 2 * qx + 6]) = top;
+        *reinterpret_cast<float2 *>(&Vp[(2 * qy + 7) * VS + 2 * qx + 6]) = bot;
+    }
+
     /* The prepped mosaic of the tile and its apron: two u32 (two samples
      * each) per quad. */
     CRAW_DEV void load(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, int y0)
@@ -344,16 +360,21 @@ struct RcdQuads {
             const char *r0 = (const char *)io.src + (size_t)y * io.src_pitch;
             uint32_t a = __ldg(reinterpret_cast<const uint32_t *>(r0) + x / 2);
             uint32_t b = __ldg(reinterpret_cast<const uint32_t *>(r0 + io.src_pitch) + x / 2);
-            float2 top, bot;
-            if (io.src_f16) {   /* rebuilt highlights: fp16, already prepped */
-                top = __half22float2(*reinterpret_cast<const __half2 *>(&a));
-                bot = __half22float2(*reinterpret_cast<const __half2 *>(&b));
-            } else {
-                top = make_float2(craw_prep(k, (uint16_t)(a & 0xffff), 0), craw_prep(k, (uint16_t)(a >> 16), 1));
-                bot = make_float2(craw_prep(k, (uint16_t)(b & 0xffff), 2), craw_prep(k, (uint16_t)(b >> 16), 3));
-            }
-            *reinterpret_cast<float2 *>(&Vp[(2 * qy + 6) * VS + 2 * qx + 6]) = top;
-            *reinterpret_cast<float2 *>(&Vp[(2 * qy + 7) * VS + 2 * qx + 6]) = bot;
+            put_quad(k, io, qx, qy, a, b);
+        }
+    }
+
+    /* The same from the tile's mosaic already in shared memory: `box` is
+     * BW 16-bit samples a row (BW even) from frame column x0 - 8 and row
+     * y0 - 6, as a TMA tile copy leaves it. */
+    template <int BW>
+    CRAW_DEV void load_box(const CRAWKDevelop &k, const CRAWKDevelopIO &io, const uint32_t *box)
+    {
+        constexpr int QX = QW + 6, QY = QH + 6;
+        for (int i = threadIdx.x; i < QX * QY; i += NT) {
+            int qx = i % QX - 3, qy = i / QX - 3;
+            const uint32_t *r0 = box + (2 * qy + 6) * (BW / 2) + qx + 4;
+            put_quad(k, io, qx, qy, r0[0], r0[BW / 2]);
         }
     }
 

@@ -151,6 +151,23 @@ def test_every_denoise_shape_vs_oracle(ctx, shape, temporal):
         L.debug_force_denoise_shape(-1)
 
 
+def test_autotuned_shapes_agree_per_size(ctx):
+    """Pipelines of one size get the same denoise shapes whatever mix of
+    stages they were created with (the tuner's picks are kept per size and
+    per kind), so that they give the same results."""
+    w, h = 1206, 610
+    seen = []
+    for flags in (L.FLAG_DENOISE, L.FLAG_DENOISE, L.FLAG_TEMPORAL_DENOISE,
+                  L.FLAG_DENOISE | L.FLAG_TEMPORAL_DENOISE, L.FLAG_DENOISE):
+        with L.Pipeline(ctx, L.pipeline_params(w, h, flags=flags)) as pipe:
+            a, b = pipe.kernel_config()
+            seen.append((a if flags & L.FLAG_DENOISE else None,
+                         b if flags & L.FLAG_TEMPORAL_DENOISE else None))
+    spatial = {s[0] for s in seen if s[0] is not None}
+    temporal = {s[1] for s in seen if s[1] is not None}
+    assert len(spatial) == 1 and len(temporal) == 1, seen
+
+
 @pytest.mark.parametrize("storage", [L.STORAGE_FP32, L.STORAGE_FP16])
 @pytest.mark.parametrize("deb", [L.DEBAYER_BILINEAR, L.DEBAYER_RCD])
 @pytest.mark.parametrize("chroma", [False, True])
