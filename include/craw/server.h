@@ -50,6 +50,16 @@ typedef struct CRAWServerParams {
  * track. Needs CRAW_PIPELINE_FLAG_AWB_HISTOGRAM and a profile with a white
  * balance table; the stream's frames then run one at a time. */
 #define CRAW_SERVER_STREAM_AUTO_WB (1u << 0)
+/* A stream without a noise model: its first frame's model is measured on
+ * the device (craw_noise_estimate_cuda on the staged mosaic, default
+ * options, before the frame develops) and is the noise override of every
+ * frame of the stream that carries none (noise_override.a <= 0). The
+ * first frame's result carries the estimate (noise_valid). A frame whose
+ * estimate fails (too few levels) fails with that error and the next frame
+ * tries again. The estimate's scratch (6 bytes a sample, freed at once)
+ * comes from the device's default memory pool, outside the budget. Needs
+ * CRAW_PIPELINE_FLAG_DENOISE or CRAW_PIPELINE_FLAG_TEMPORAL_DENOISE. */
+#define CRAW_SERVER_STREAM_ESTIMATE_NOISE (1u << 1)
 
 typedef struct CRAWServerStreamParams {
     CRAWPipelineParams pipeline;   /* frame size, debayer, output, stages */
@@ -69,6 +79,8 @@ typedef struct CRAWServerResult {
     bool awb_valid;                /* AUTO_WB: the track after this frame */
     CRAWIlluminant awb;
     CRAWAwbEstimate estimate;      /* AUTO_WB: this frame's own reading */
+    bool noise_valid;              /* ESTIMATE_NOISE: measured on this frame */
+    CRAWNoiseEstimate noise;
 } CRAWServerResult;
 
 typedef struct CRAWServerStats {

@@ -233,7 +233,8 @@ class ServerStreamParams(C.Structure):
 class ServerResult(C.Structure):
     _fields_ = [("user", C.c_uint64), ("stream", C.c_uint32), ("status", C.c_int),
                 ("queue_ms", C.c_double), ("latency_ms", C.c_double), ("device_ms", C.c_double),
-                ("awb_valid", C.c_bool), ("awb", Illuminant), ("estimate", AwbEstimate)]
+                ("awb_valid", C.c_bool), ("awb", Illuminant), ("estimate", AwbEstimate),
+                ("noise_valid", C.c_bool), ("noise", NoiseEstimate)]
 
 
 class ServerStats(C.Structure):
@@ -244,6 +245,7 @@ class ServerStats(C.Structure):
 
 
 SERVER_STREAM_AUTO_WB = 1 << 0
+SERVER_STREAM_ESTIMATE_NOISE = 1 << 1
 
 
 class BatchParams(C.Structure):
@@ -260,7 +262,8 @@ class BatchInfo(C.Structure):
 for _s, _n in ((Profile, 1264), (FrameParams, 264), (PipelineParams, 256), (CudaInitParams, 64),
                (ContextOptions, 1024), (LensCorrection, 64), (BatchParams, 64), (AwbParams, 36),
                (AwbCandidate, 20), (AwbEstimate, 68), (AwbSmootherParams, 16), (ServerParams, 64),
-               (ServerStreamParams, 376), (ServerResult, 120)):
+               (ServerStreamParams, 376), (ServerResult, 192), (NoiseEstimateParams, 64),
+               (NoiseEstimate, 64)):
     assert C.sizeof(_s) == _n, (_s.__name__, C.sizeof(_s), _n)
 
 # ----------------------------------------------------------------- library

@@ -39,6 +39,7 @@ struct job {
     uint64_t user;
     uint64_t seq;                    /* submission order within the server */
     double t_submit, t_launch;
+    bool noise_measured;             /* the stream's noise model came from this frame */
 };
 
 struct slot {
@@ -63,6 +64,8 @@ struct stream {
     CRAWAwbSmoother *sm;
     bool have_track;
     CRAWIlluminant track;
+    bool have_noise;                 /* ESTIMATE_NOISE: measured */
+    CRAWNoiseEstimate noise;
 };
 
 struct CRAWServer {
@@ -211,6 +214,18 @@ static int launch(CRAWServer *s, struct stream *st, struct slot *sl, struct job 
         cudaMemcpy2DAsync(sl->src_dev, sl->src_pitch, j->src, j->src_pitch, (size_t)pp->width * 2,
                           pp->height, cudaMemcpyDefault, st->cs) != cudaSuccess)
         return CRAW_ERROR(EIO);
+    if (st->params.flags & CRAW_SERVER_STREAM_ESTIMATE_NOISE) {
+        /* Once per stream; the call waits for the copy above and returns
+         * with the estimate (the worker holds the lock meanwhile). */
+        if (!st->have_noise) {
+            if ((ret = craw_noise_estimate_cuda(&src, fp.profile, NULL, &st->noise, st->cs)) < 0)
+                return ret;
+            st->have_noise = true;
+            j->noise_measured = true;
+        }
+        if (!(fp.noise_override.a > 0.0f))
+            fp.noise_override = st->noise.model;
+    }
     if ((ret = craw_pipeline_record(st->pipe, st->cs, &src, &dst, &fp)) < 0)
         return ret;
     if (cudaMemcpy2DAsync(j->dst, j->dst_pitch, sl->dst_dev, sl->dst_pitch,
@@ -345,6 +360,10 @@ static bool retire_done(CRAWServer *s)
             r.status = e == cudaSuccess ? 0 : CRAW_ERROR(EIO);
             if (e == cudaSuccess && cudaEventElapsedTime(&dev_ms, sl->ev0, sl->ev1) == cudaSuccess)
                 r.device_ms = dev_ms;
+            if (j->noise_measured) {
+                r.noise_valid = true;
+                r.noise = st->noise;
+            }
             if (r.status == 0 && (st->params.flags & CRAW_SERVER_STREAM_AUTO_WB)) {
                 st->busy_host = true;
                 pthread_mutex_unlock(&s->lock);
@@ -511,9 +530,14 @@ CRAW_API int craw_server_stream_open(CRAWServer *s, const CRAWServerStreamParams
     pp = &params->pipeline;
     if (pp->out_format != CRAW_FORMAT_RGBA16F && pp->out_format != CRAW_FORMAT_RGBA32F)
         return CRAW_ERROR(EINVAL);
-    if ((params->flags & ~CRAW_SERVER_STREAM_AUTO_WB) ||
+    if ((params->flags & ~(CRAW_SERVER_STREAM_AUTO_WB | CRAW_SERVER_STREAM_ESTIMATE_NOISE)) ||
         ((params->flags & CRAW_SERVER_STREAM_AUTO_WB) && !(pp->flags & CRAW_PIPELINE_FLAG_AWB_HISTOGRAM))) {
         craw_log(s->ctx, CRAW_LOG_ERROR, "server: AUTO_WB needs CRAW_PIPELINE_FLAG_AWB_HISTOGRAM\n");
+        return CRAW_ERROR(EINVAL);
+    }
+    if ((params->flags & CRAW_SERVER_STREAM_ESTIMATE_NOISE) &&
+        !(pp->flags & (CRAW_PIPELINE_FLAG_DENOISE | CRAW_PIPELINE_FLAG_TEMPORAL_DENOISE))) {
+        craw_log(s->ctx, CRAW_LOG_ERROR, "server: ESTIMATE_NOISE needs a denoising pipeline\n");
         return CRAW_ERROR(EINVAL);
     }
     if (!(st = calloc(1, sizeof(*st))))

@@ -228,6 +228,47 @@ def test_auto_wb_closed_loop(ctx):
         assert np.array_equal(feed.dst[i].numpy(), want), i
 
 
+def test_estimate_noise_for_a_stream_without_a_model(ctx):
+    """With ESTIMATE_NOISE the first frame's model is measured on the
+    device (equal to craw_noise_estimate of that frame) and every frame
+    without an override is developed with it: the same as developing it
+    directly with that model. A stream of frames too flat to fit fails its
+    frame with ENODATA and tries again on the next."""
+    prof = W.make_profile()
+    w, h = 2560, 1440            # enough samples for the default 20000 a bin
+    ms = [W.noise_ramp(w, h, 900 + i, lo=0.0) for i in range(3)]
+    pp = pipeline_params(w, h, temporal=False)
+    fp = L.frame_params(prof, denoise_strength=1.0)          # no model: estimated
+    est0 = L.noise_estimate(ms[0], prof)
+    with L.Server(ctx, L.server_params(hbm_budget=8 << 30)) as srv:
+        sid = srv.open(L.server_stream_params(pp, L.SERVER_STREAM_ESTIMATE_NOISE))
+        feed = Feed(ms)
+        for i in range(len(ms)):
+            feed.submit(srv, sid, i, fp)
+        srv.drain()
+        res = sorted(srv.poll(16), key=lambda r: r.user)
+        assert [r.status for r in res] == [0, 0, 0]
+        assert [r.noise_valid for r in res] == [True, False, False]
+        assert res[0].noise.as_tuple() == est0.as_tuple()
+        fpm = L.frame_params(prof, denoise_strength=1.0, noise_override=(est0.model.a, est0.model.b))
+        want = direct(ctx, ms, pp, fpm)
+        for i in range(len(ms)):
+            assert np.array_equal(feed.dst[i].numpy(), want[i]), i
+
+        flat = [np.full((h, w), W.BLACK_DN + 900, np.uint16)] + ms[:1]
+        sid2 = srv.open(L.server_stream_params(pp, L.SERVER_STREAM_ESTIMATE_NOISE))
+        feed2 = Feed(flat)
+        for i in range(2):
+            feed2.submit(srv, sid2, i, fp)
+        srv.drain()
+        res2 = sorted(srv.poll(16), key=lambda r: r.user)
+        assert res2[0].status == -errno.ENODATA and not res2[0].noise_valid
+        assert res2[1].status == 0 and res2[1].noise_valid
+    with L.Server(ctx, L.server_params(hbm_budget=8 << 30)) as srv:
+        with pytest.raises(L.CrawError):
+            srv.open(L.server_stream_params(L.pipeline_params(w, h), L.SERVER_STREAM_ESTIMATE_NOISE))
+
+
 def test_server_errors(ctx):
     prof = W.make_profile()
     with L.Server(ctx, L.server_params(hbm_budget=1 << 30)) as srv:
