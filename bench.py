@@ -444,7 +444,9 @@ def run_gpu(args):
                 "64 frames of 640x360 (previews), NLM 1.0 + RCD + BT.2020 float32")
             if base:
                 extras["batch"]["eq_speedup_vs_plain_fp32"] = (
-                    extras["batch"]["fused_graph"]["eq_5760x3240_fps"] / base)
+                    extras["batch"]["split_default"]["eq_5760x3240_fps"] / base)
+                extras["batch"]["persistent_eq_speedup_vs_plain_fp32"] = (
+                    extras["batch"]["unfused_graph"]["eq_5760x3240_fps"] / base)
         if "temporal" in want:
             extras["temporal_seq"] = run_temporal_seq(ctx, stream)
         if "serve" in want:
@@ -544,13 +546,25 @@ def run_batch_mix(ctx, stream, steps: int, warmup: int, mix=None, label: str | N
     res = {"workload": label or ("16 frames: 6x1920x1080, 4x3840x2160, 4x5760x3240, 2x6000x4000; "
                                  "NLM 1.0 + RCD + BT.2020 float32; noise a~U[1,8], b~U[10,80] per frame"),
            "mpx": n_px / 1e6}
-    for name, flags in (("fused_graph", 0), ("unfused_graph", L.BATCH_FLAG_UNFUSED),
-                        ("fused_no_graph", L.BATCH_FLAG_NO_GRAPH)):
+    # Every frame in the persistent launch (one fused launch with a grid
+    # barrier, two launches, without a graph), then the default plan: two
+    # persistent launches from a graph for the frames under 4 Mpx, the
+    # larger ones through the single-frame kernels after them.
+    for name, flags, direct in (("fused_graph", L.BATCH_FLAG_FUSED, L.BATCH_ALL_PERSISTENT),
+                                ("unfused_graph", L.BATCH_FLAG_UNFUSED, L.BATCH_ALL_PERSISTENT),
+                                ("fused_no_graph", L.BATCH_FLAG_FUSED | L.BATCH_FLAG_NO_GRAPH,
+                                 L.BATCH_ALL_PERSISTENT),
+                                ("split_default", 0, 0)):
         bp = L.batch_params(mw, mh, max_frames=len(mix), debayer=L.DEBAYER_RCD,
-                            out_space=L.CS_BT2020, flags=L.FLAG_DENOISE | flags)
+                            out_space=L.CS_BT2020, flags=L.FLAG_DENOISE | flags, direct_pixels=direct)
         with L.Batch(ctx, bp) as b:
             res[name] = timed(lambda: b.record(sptr, srcs, dsts, fps))
-            res[name]["denoise_tile"] = ["2x4", "2x8"][b.info()["denoise_shape"]]
+            info = b.info()
+            res[name]["denoise_tile"] = ["2x4", "2x8"][info["denoise_shape"]]
+            if info["direct_frames"]:
+                res[name]["direct_frames_per_batch"] = sum(
+                    1 for f in mix if f.width * f.height >= L.BATCH_DIRECT_PIXELS)
+                res[name]["direct_denoise_tile"] = L.DN_SHAPES[info["direct_shape"]]
     pipes = {}
     for f in mix:
         if (f.width, f.height) not in pipes:
@@ -564,8 +578,10 @@ def run_batch_mix(ctx, stream, steps: int, warmup: int, mix=None, label: str | N
     res["single_frame_pipeline"] = timed(singles)
     for p_ in pipes.values():
         p_.close()
-    res["speedup_vs_single_frames"] = (res["fused_graph"]["frames_per_s"] /
+    res["speedup_vs_single_frames"] = (res["unfused_graph"]["frames_per_s"] /
                                        res["single_frame_pipeline"]["frames_per_s"])
+    res["split_speedup_vs_single_frames"] = (res["split_default"]["frames_per_s"] /
+                                             res["single_frame_pipeline"]["frames_per_s"])
     return res
 
 

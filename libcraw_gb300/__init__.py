@@ -58,6 +58,7 @@ FLAG_KEEP_INTERMEDIATE = 1 << 16
 FLAG_NO_AUTOTUNE = 1 << 17
 BATCH_FLAG_UNFUSED = 1 << 20
 BATCH_FLAG_NO_GRAPH = 1 << 21
+BATCH_FLAG_FUSED = 1 << 22
 
 FRAME_CLAMP_NEGATIVE = 1 << 0
 FRAME_NO_GAMUT_COMPRESSION = 1 << 2
@@ -251,12 +252,20 @@ SERVER_STREAM_ESTIMATE_NOISE = 1 << 1
 class BatchParams(C.Structure):
     _fields_ = [("max_frames", C.c_uint32), ("max_width", C.c_uint32), ("max_height", C.c_uint32),
                 ("debayer", C.c_int), ("out_space", C.c_int), ("out_format", C.c_int),
-                ("flags", C.c_uint32), ("padding", C.c_uint8 * 36)]
+                ("flags", C.c_uint32), ("direct_pixels", C.c_uint32), ("padding", C.c_uint8 * 32)]
+
+
+#: Frames of a batch with at least this many pixels go to the single-frame
+#: kernels (BatchParams.direct_pixels = 0); BATCH_ALL_PERSISTENT keeps every
+#: frame in the persistent launch.
+BATCH_DIRECT_PIXELS = 4000000
+BATCH_ALL_PERSISTENT = 0xFFFFFFFF
 
 
 class BatchInfo(C.Structure):
     _fields_ = [("denoise_shape", C.c_int), ("fused", C.c_int), ("graph", C.c_int),
-                ("captures", C.c_uint64), ("replays", C.c_uint64)]
+                ("captures", C.c_uint64), ("replays", C.c_uint64), ("direct_shape", C.c_int),
+                ("direct_frames", C.c_uint64)]
 
 
 for _s, _n in ((Profile, 1264), (FrameParams, 264), (PipelineParams, 256), (CudaInitParams, 64),
@@ -817,7 +826,8 @@ class Batch:
         i = BatchInfo()
         _check(lib().craw_batch_get_info(self._h, C.byref(i)), "craw_batch_get_info")
         return {"denoise_shape": i.denoise_shape, "fused": bool(i.fused), "graph": bool(i.graph),
-                "captures": i.captures, "replays": i.replays}
+                "captures": i.captures, "replays": i.replays, "direct_shape": i.direct_shape,
+                "direct_frames": i.direct_frames}
 
     def close(self) -> None:
         if self._h:

@@ -32,6 +32,11 @@ struct CRAWBatch {
     bool sig_dn[BATCH_MAX];
     int32_t sig_dn_items, sig_dv_items;
     uint64_t captures, replays;
+    /* Frames developed by the single-frame kernels. */
+    uint64_t direct_pixels;
+    int direct_shape;                /* their denoise tile shape, autotuned; -1: none */
+    uint64_t direct_frames;
+    CRAWKBatchFrame direct[BATCH_MAX];
 };
 
 CRAW_API void craw_batch_params_init(CRAWBatchParams *p)
@@ -162,6 +167,35 @@ static int batch_autotune(CRAWBatch *b)
     craw_log(ctx, CRAW_LOG_VERBOSE, "batch autotune %ux%u: denoise shape %d, %.3f ms\n", w, h,
              b->shape, (double)best);
     ret = 0;
+    /* The single-frame kernel's shapes, for frames developed directly. */
+    b->direct_shape = -1;
+    if ((uint64_t)w * h >= b->direct_pixels) {
+        best = 1e30f;
+        for (int shape = 0; shape < CRAW_K_DN_SHAPE_NB; shape++) {
+            float t = 0.0f, ms = 1e30f;
+            for (int r = 0; r < 3; r++) {
+                cudaEventRecord(e0, ctx->stream);
+                if (craw_k_denoise(&F->dn, &F->dio, shape, ctx->stream) < 0) {
+                    ret = CRAW_ERROR(EIO);
+                    goto done;
+                }
+                cudaEventRecord(e1, ctx->stream);
+                if (cudaEventSynchronize(e1) != cudaSuccess ||
+                    cudaEventElapsedTime(&t, e0, e1) != cudaSuccess) {
+                    ret = CRAW_ERROR(EIO);
+                    goto done;
+                }
+                if (r > 0 && t < ms)
+                    ms = t;
+            }
+            if (ms < best) {
+                best = ms;
+                b->direct_shape = shape;
+            }
+        }
+        craw_log(ctx, CRAW_LOG_VERBOSE, "batch autotune %ux%u: direct denoise shape %d, %.3f ms\n", w, h,
+                 b->direct_shape, (double)best);
+    }
 done:
     if (e0)
         cudaEventDestroy(e0);
@@ -188,8 +222,9 @@ CRAW_API int craw_batch_create(CRAWContext *ctx, const CRAWBatchParams *params, 
         (unsigned)params->out_space >= CRAW_CS_NB ||
         (params->out_format != CRAW_FORMAT_RGBA16F && params->out_format != CRAW_FORMAT_RGBA32F))
         return CRAW_ERROR(EINVAL);
-    if (params->flags & ~(uint32_t)(CRAW_PIPELINE_FLAG_DENOISE | CRAW_BATCH_FLAG_UNFUSED |
-                                     CRAW_BATCH_FLAG_NO_GRAPH)) {
+    if ((params->flags & ~(uint32_t)(CRAW_PIPELINE_FLAG_DENOISE | CRAW_BATCH_FLAG_UNFUSED |
+                                      CRAW_BATCH_FLAG_FUSED | CRAW_BATCH_FLAG_NO_GRAPH)) ||
+        ((params->flags & CRAW_BATCH_FLAG_FUSED) && (params->flags & CRAW_BATCH_FLAG_UNFUSED))) {
         craw_log(ctx, CRAW_LOG_ERROR, "Batch flags 0x%x: only the denoise is supported in a batch\n",
                  params->flags);
         return CRAW_ERROR(ENOTSUP);
@@ -199,9 +234,12 @@ CRAW_API int craw_batch_create(CRAWContext *ctx, const CRAWBatchParams *params, 
         return CRAW_ERROR(ENOMEM);
     b->ctx = ctx;
     b->params = *params;
-    b->fused = !(params->flags & CRAW_BATCH_FLAG_UNFUSED);
+    b->fused = (params->flags & CRAW_BATCH_FLAG_FUSED) != 0;
     b->use_graph = !(params->flags & CRAW_BATCH_FLAG_NO_GRAPH);
     b->denoise = params->flags & CRAW_PIPELINE_FLAG_DENOISE;
+    b->direct_pixels = params->direct_pixels == UINT32_MAX ? UINT64_MAX :
+                       (params->direct_pixels ? params->direct_pixels : CRAW_BATCH_DIRECT_PIXELS);
+    b->direct_shape = -1;
     cudaSetDevice(ctx->device);
 
     b->clean_pitch = (((size_t)params->max_width * 2) + 255) / 256 * 256;
@@ -246,6 +284,8 @@ CRAW_API int craw_batch_get_info(CRAWBatch *b, CRAWBatchInfo *info)
     info->graph = b->use_graph;
     info->captures = b->captures;
     info->replays = b->replays;
+    info->direct_shape = b->direct_shape;
+    info->direct_frames = b->direct_frames;
     return 0;
 }
 
@@ -280,6 +320,9 @@ static int batch_capture(CRAWBatch *b, uint32_t nb, int32_t dn_items, int32_t dv
     return 0;
 }
 
+static int batch_persistent(CRAWBatch *b, cudaStream_t s, uint32_t nb, const uint32_t *w, const uint32_t *h,
+                            const bool *dn);
+
 CRAW_API int craw_batch_record(CRAWBatch *b, cudaStream_t s, uint32_t nb, const CRAWImage *src,
                                const CRAWImage *dst, const CRAWFrameParams *fp)
 {
@@ -287,8 +330,6 @@ CRAW_API int craw_batch_record(CRAWBatch *b, cudaStream_t s, uint32_t nb, const 
     CRAWKBatchFrame *F;
     uint32_t w[BATCH_MAX], h[BATCH_MAX];
     bool dn[BATCH_MAX];
-    int32_t dn_items, dv_items;
-    bool same;
     int ret;
 
     if (!b || !src || !dst || !fp || !nb)
@@ -340,6 +381,48 @@ CRAW_API int craw_batch_record(CRAWBatch *b, cudaStream_t s, uint32_t nb, const 
         F[i].vio.dst_pitch = dst[i].pitch;
         F[i].vio.dst_half = dst[i].format == CRAW_FORMAT_RGBA16F;
     }
+
+    /* Large frames go to the single-frame kernels; the others, in order,
+     * stay in the table of the persistent launch. */
+    uint32_t nd = 0, ns = 0;
+    bool ddn[BATCH_MAX];
+    for (uint32_t i = 0; i < nb; i++) {
+        if ((uint64_t)w[i] * h[i] >= b->direct_pixels) {
+            b->direct[nd] = F[i];
+            ddn[nd++] = dn[i];
+            continue;
+        }
+        if (ns != i) {
+            F[ns] = F[i];
+            w[ns] = w[i];
+            h[ns] = h[i];
+            dn[ns] = dn[i];
+        }
+        ns++;
+    }
+    if (ns > 0 && (ret = batch_persistent(b, s, ns, w, h, dn)) < 0)
+        return ret;
+    for (uint32_t d = 0; d < nd; d++) {
+        if ((ddn[d] && craw_k_denoise(&b->direct[d].dn, &b->direct[d].dio, b->direct_shape, s) < 0) ||
+            craw_k_develop(&b->direct[d].dv, &b->direct[d].vio, 0, s) < 0)
+            return CRAW_ERROR(EIO);
+        b->direct_frames++;
+    }
+    return 0;
+}
+
+/* The persistent launch of frames 0 .. nb-1 of the table: a replay of the
+ * graph captured for these shapes (captured now if they are new), or a
+ * launch. */
+static int batch_persistent(CRAWBatch *b, cudaStream_t s, uint32_t nb, const uint32_t *w, const uint32_t *h,
+                            const bool *dn)
+{
+    CRAWContext *ctx = b->ctx;
+    CRAWKBatchFrame *F = b->table->f;
+    int32_t dn_items, dv_items;
+    bool same;
+    int ret;
+
     batch_layout(b, nb, w, h, dn, F, &dn_items, &dv_items);
 
     same = b->exec && b->sig_nb == nb;

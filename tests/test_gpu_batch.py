@@ -87,6 +87,26 @@ def test_batch_matches_single_frames(ctx, deb):
     check_against_single(ctx, got, ms, fps, deb, L.FLAG_DENOISE)
 
 
+def test_split_plan_matches_single_frames(ctx):
+    """With a low direct_pixels the larger frames go to the single-frame
+    kernels after the persistent launch of the others: the results are the
+    single-frame pipeline's all the same, and a replay repeats them."""
+    prof = W.make_profile()
+    ms = frames(300)
+    fps = [params(prof, i, True) for i in range(len(ms))]
+    bp = L.batch_params(1030, 352, max_frames=8, debayer=L.DEBAYER_RCD, out_space=L.CS_ACES_AP1,
+                        flags=L.FLAG_DENOISE, direct_pixels=100000)
+    with L.Batch(ctx, bp) as b:
+        got = run_batch(b, ms, fps)
+        info = b.info()
+        assert info["direct_frames"] == sum(1 for w, h in SIZES if w * h >= 100000) == 2
+        assert 0 <= info["direct_shape"] < len(L.DN_SHAPES)
+        again = run_batch(b, ms, fps)
+        assert all(np.array_equal(a, c) for a, c in zip(got, again))
+        assert b.info()["captures"] == 1
+    check_against_single(ctx, got, ms, fps, L.DEBAYER_RCD, L.FLAG_DENOISE)
+
+
 def test_batch_vs_oracle(ctx):
     """The transitive check made direct: batch frames against the oracle."""
     prof = W.make_profile()
@@ -137,12 +157,13 @@ def test_fused_unfused_graph_agree(ctx):
     ms = frames(500)
     fps = [params(prof, i, True) for i in range(len(ms))]
     outs = []
-    for flags in (0, L.BATCH_FLAG_UNFUSED, L.BATCH_FLAG_NO_GRAPH,
-                  L.BATCH_FLAG_UNFUSED | L.BATCH_FLAG_NO_GRAPH):
+    for flags in (L.BATCH_FLAG_FUSED, L.BATCH_FLAG_UNFUSED, L.BATCH_FLAG_NO_GRAPH,
+                  L.BATCH_FLAG_FUSED | L.BATCH_FLAG_NO_GRAPH):
         bp = L.batch_params(1030, 352, max_frames=8, debayer=L.DEBAYER_RCD,
                             out_space=L.CS_ACES_AP1, flags=L.FLAG_DENOISE | flags)
         with L.Batch(ctx, bp) as b:
             outs.append((run_batch(b, ms, fps), b.info()))
+    assert [o[1]["fused"] for o in outs] == [True, False, False, True]
     for o, info in outs[1:]:
         for a, c in zip(outs[0][0], o):
             if info["denoise_shape"] == outs[0][1]["denoise_shape"]:
