@@ -526,6 +526,10 @@ struct RcdQuads {
 
 /* ------------------------------------------------------------- epilogue */
 
+template <int TW, int TH, int NTH>
+CRAW_DEV void awb_blocks(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, int y0, const float *rgb,
+                         int t);
+
 /* From the tile's camera RGB (planar in shared memory, fp32, complete):
  * the intermediate as it would be stored, then the colour stage into dst,
  * or the chroma block means, and the AWB block records. */
@@ -535,7 +539,17 @@ CRAW_DEV void epilogue(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, 
     constexpr int P = TW * TH;
     static_assert(P % 4 == 0 && TW % 8 == 0, "planes and block rows are whole float4s");
     const bool chroma = io.quarter != nullptr;
-    for (int i = threadIdx.x; i < P; i += NT) {
+    /* With FP32 storage the AWB block sums read what the debayer left, so
+     * the last warp makes them while the others run the colour stage: the
+     * sums are long sequential chains over a few threads, and the tile's
+     * slot on the SM is held until they end. */
+    const bool awb_apart = !k.fp16 && !chroma && io.awb.rec && NT > 64;
+    const int ncol = awb_apart ? NT - 32 : NT;
+    if (awb_apart && (int)threadIdx.x >= ncol) {
+        awb_blocks<TW, TH, 32>(k, io, x0, y0, rgb, threadIdx.x - ncol);
+        return;
+    }
+    for (int i = threadIdx.x; i < P; i += ncol) {
         int x = x0 + i % TW, y = y0 + i / TW;
         float v[3] = { rgb[i], rgb[P + i], rgb[2 * P + i] };
         if (k.fp16) {
@@ -555,7 +569,7 @@ CRAW_DEV void epilogue(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, 
             craw_store_rgba(io.dst, io.dst_pitch, x, y, io.dst_half, o[0], o[1], o[2]);
         }
     }
-    if (!chroma && !io.awb.rec)
+    if ((!chroma && !io.awb.rec) || awb_apart)
         return;
     if (k.fp16)
         __syncthreads();
@@ -588,9 +602,18 @@ CRAW_DEV void epilogue(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, 
         return;
     }
 
-    /* 8x8 block means, row by row (reference lib/awb.c:239-253). */
+    awb_blocks<TW, TH, NT>(k, io, x0, y0, rgb, threadIdx.x);
+}
+
+/* The AWB records of the tile's 8x8 blocks, block means summed row by row
+ * (reference lib/awb.c:239-253); thread t of NTH takes blocks t, t + NTH, ... */
+template <int TW, int TH, int NTH>
+CRAW_DEV void awb_blocks(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, int y0, const float *rgb,
+                         int t)
+{
+    constexpr int P = TW * TH;
     const int blocks_x = (k.width + 7) / 8;
-    for (int b = threadIdx.x; b < (TW / 8) * (TH / 8); b += NT) {
+    for (int b = t; b < (TW / 8) * (TH / 8); b += NTH) {
         int bx = b % (TW / 8), by = b / (TW / 8);
         if (x0 + bx * 8 >= k.width || y0 + by * 8 >= k.height)
             continue;
