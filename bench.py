@@ -232,7 +232,7 @@ def run_reference(args):
     from libcraw_gb300 import build as B
     from libcraw_gb300 import workloads as W
     B.build()
-    c = W.config(2, args.width, args.height)
+    c = W.workload("nlm_rcd_ap1", args.width, args.height)
     frame = c.frame()
     prof = W.make_profile()
     pp = L.pipeline_params(c.width, c.height, debayer=c.debayer, out_space=c.out_space, flags=c.flags,
@@ -253,7 +253,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": value, "unit": "frames/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": total / args.steps * 1000, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded generator, config 2)",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic: the seeded generator's 5760x3240 frames",
         "config": {"workload": WORKLOAD, "width": c.width, "height": c.height},
         "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))]},
         "cpu_baseline": {**last, "value": value},
@@ -279,7 +279,7 @@ def run_gpu(args):
     dev = torch.cuda.current_device()
     props = torch.cuda.get_device_properties(dev)
 
-    c = W.config(2, args.width, args.height)
+    c = W.workload("nlm_rcd_ap1", args.width, args.height)
     w, h = c.width, c.height
     prof = W.make_profile()
     fp = L.frame_params(prof, **c.frame_kwargs())
@@ -595,7 +595,7 @@ def run_highlights(ctx, stream, nsteps: int = 20) -> dict:
     import libcraw_gb300 as L
     from libcraw_gb300 import workloads as W
 
-    c = W.config(2)
+    c = W.workload("nlm_rcd_ap1")
     w, h = c.width, c.height
     prof = W.make_profile()
     fp = L.frame_params(prof, flags=L.FRAME_HIGHLIGHT_RECONSTRUCTION, **c.frame_kwargs())
@@ -637,7 +637,7 @@ def run_noise_estimate(nsteps: int = 10, cpu: bool = True) -> dict:
     import libcraw_gb300 as L
     from libcraw_gb300 import workloads as W
 
-    c = W.config(2)
+    c = W.workload("nlm_rcd_ap1")
     w, h = c.width, c.height
     prof = W.make_profile()
     frame = c.frame(0)
@@ -683,7 +683,7 @@ def run_temporal_seq(ctx, stream, nsteps: int = 60, distinct: int = 12) -> dict:
     import libcraw_gb300 as L
     from libcraw_gb300 import workloads as W
 
-    c = W.config(3)
+    c = W.workload("temporal_mhc_p3")
     w, h = c.width, c.height
     prof = W.make_profile()
     fp = L.frame_params(prof, **c.frame_kwargs())

@@ -132,32 +132,37 @@ class Config:
         return kw
 
 
-def config(n: int, width: int | None = None, height: int | None = None) -> Config:
-    """Benchmark configuration ``n`` (1-based as listed), optionally at
-    another size (the tests run them small)."""
-    if n == 1:   # plain method: bilinear, no denoise, BT.709
+#: The benchmark workloads by name.
+WORKLOADS = ("bilinear_bt709_1080p", "nlm_rcd_ap1", "temporal_mhc_p3", "batch_rcd_bt2020",
+             "serve_rcd_ap0")
+
+
+def workload(name: str, width: int | None = None, height: int | None = None) -> Config:
+    """Benchmark workload `name` (one of WORKLOADS), optionally at another
+    size (the tests run them small)."""
+    if name == "bilinear_bt709_1080p":   # bilinear, no denoise, BT.709
         c = Config("1920x1080 bilinear BT.709", 1920, 1080, 1001, 64, 1, 2.0, 16.0,
                    DEBAYER_BILINEAR, CS_BT709, FLAG_AWB_HISTOGRAM)
-    elif n == 2:  # full chain, single frame
+    elif name == "nlm_rcd_ap1":          # the full chain on one frame
         c = Config("5760x3240 VST+NLM1.0+RCD+AP1+AWB", 5760, 3240, 2002, 256, 4, 4.0, 40.0,
                    DEBAYER_RCD, CS_ACES_AP1, FLAG_AWB_HISTOGRAM | FLAG_DENOISE,
                    denoise_strength=1.0)
-    elif n == 3:  # temporal sequence
+    elif name == "temporal_mhc_p3":      # a temporal sequence with movers
         c = Config("5760x3240 x60 temporal0.8+NLM1.0+chroma0.5+MHC+P3", 5760, 3240, 3003, 256, 4,
                    4.0, 40.0, DEBAYER_MHC, CS_P3D65,
                    FLAG_AWB_HISTOGRAM | FLAG_DENOISE | FLAG_TEMPORAL_DENOISE | FLAG_CHROMA_DENOISE,
                    denoise_strength=1.0, temporal_strength=0.8, chroma_strength=0.5, frames=60,
                    movers=[(2.0, 0.5), (8.0, 2.0), (24.0, 10.0)])
-    elif n == 4:  # batched uneven sizes (one frame of the mix here)
+    elif name == "batch_rcd_bt2020":     # one frame of the uneven batch
         c = Config("batch NLM1.0+RCD+BT.2020", 5760, 3240, 4004, 256, 4, 4.0, 40.0,
                    DEBAYER_RCD, CS_BT2020, FLAG_AWB_HISTOGRAM | FLAG_DENOISE, denoise_strength=1.0)
-    elif n == 5:  # serving
+    elif name == "serve_rcd_ap0":        # one frame of a served clip
         c = Config("serve temporal0.8+NLM+RCD+AP0", 5760, 3240, 5005, 256, 4, 4.0, 40.0,
                    DEBAYER_RCD, CS_ACES_AP0,
                    FLAG_AWB_HISTOGRAM | FLAG_DENOISE | FLAG_TEMPORAL_DENOISE,
                    denoise_strength=1.0, temporal_strength=0.8)
     else:
-        raise ValueError(n)
+        raise ValueError(name)
     if width:
         c.width = width
     if height:

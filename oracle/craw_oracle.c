@@ -3,7 +3,7 @@
  * reference's CPU implementation (lib/ref, and the host colour/noise/AWB
  * code it calls), in float and in double.
  *
- * TEST INFRASTRUCTURE ONLY -- the checker, never the product. Only the
+ * TEST INFRASTRUCTURE ONLY -- the oracle, never the product. Only the
  * tests, the smoke check and bench.py's CPU-baseline leg load it. The
  * float instantiation is pinned against the reference's own build
  * (oracle/_ref, tests/golden) by the CPU test suite.

@@ -5,9 +5,9 @@
  * reference's float arithmetic operation for operation, and in double, the
  * FP64 run the GPU results are also measured against.
  *
- * TEST INFRASTRUCTURE ONLY. This file is the checker: only tests/, the
- * smoke check and the CPU-baseline leg of bench.py may use it, and never
- * as the thing measured or shipped.
+ * TEST INFRASTRUCTURE ONLY: only tests/, the smoke check and the
+ * CPU-baseline leg of bench.py may use it, as the oracle the GPU results
+ * are compared with, and never as the thing measured or shipped.
  *
  * Every function cites the reference file:line it restates.
  * Expected macros: R (float or double), SFX(name) (name##_f32 / _f64),

@@ -2,7 +2,7 @@
 double) and of the reference's own CPU code (oracle/_ref/libcraw_ref.so,
 present only where the reference tree was available to build it).
 
-Test infrastructure: the checker, never the thing measured. The structs
+Test infrastructure: the oracle, never the thing measured. The structs
 are those of libcraw_gb300, byte compatible with the reference's.
 """
 from __future__ import annotations

@@ -178,7 +178,7 @@ def test_recordings_in_flight(ctx):
 
 def test_determinism(ctx):
     w, h = 200, 120
-    c = W.config(2, w, h)
+    c = W.workload("nlm_rcd_ap1", w, h)
     m = c.frame()
     prof = W.make_profile()
     pp = L.pipeline_params(w, h, debayer=L.DEBAYER_RCD, flags=c.flags, out_format=L.FORMAT_RGBA32F)

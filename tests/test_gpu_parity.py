@@ -71,7 +71,7 @@ def test_full_chain_vs_oracle(ctx, impl):
     """The single-frame chain of the headline workload at a small size:
     VST + NLM 1.0 + RCD + ACES AP1 (with RGC) + AWB."""
     w, h = 256, 160
-    c = W.config(2, w, h)
+    c = W.workload("nlm_rcd_ap1", w, h)
     m = c.frame()
     prof = W.make_profile()
     pp = L.pipeline_params(w, h, debayer=c.debayer, out_space=c.out_space, flags=c.flags,
@@ -202,7 +202,7 @@ def test_awb_bit_exact(ctx, deb, storage, chroma):
 
 def test_chroma_vs_oracle(ctx):
     w, h = 240, 160
-    c = W.config(3, w, h)
+    c = W.workload("temporal_mhc_p3", w, h)
     m = c.frame()
     prof = W.make_profile()
     pp = L.pipeline_params(w, h, debayer=L.DEBAYER_MHC, out_space=L.CS_P3D65,
@@ -219,7 +219,7 @@ def test_temporal_sequence_vs_oracle(ctx):
     denoised mosaic, the state and the output follow the oracle's chain."""
     from gpu_util import download_image, upload_mosaic, alloc_rgba
     w, h = 160, 112
-    c = W.config(3, w, h)
+    c = W.workload("temporal_mhc_p3", w, h)
     prof = W.make_profile()
     model = W.noise_model(c.noise_a_dn, c.noise_b_dn)
     pp = L.pipeline_params(w, h, debayer=L.DEBAYER_MHC, out_space=L.CS_P3D65,
@@ -250,7 +250,7 @@ def test_temporal_sequence_vs_oracle(ctx):
 
 def test_plain_and_fused_agree(ctx):
     w, h = 256, 144
-    c = W.config(2, w, h)
+    c = W.workload("nlm_rcd_ap1", w, h)
     m = c.frame()
     prof = W.make_profile()
     fp = L.frame_params(prof, **c.frame_kwargs())
