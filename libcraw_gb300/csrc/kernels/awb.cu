@@ -59,13 +59,10 @@ k_awb_reduce(const uint64_t *__restrict__ rec, uint32_t n, uint32_t *__restrict_
 extern "C" int craw_k_awb_reduce(const uint64_t *rec, uint32_t n, uint32_t *hist, cudaStream_t s)
 {
     (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
-    static bool attr_set = false;
+    static std::atomic<uint64_t> attr_done{ 0 };
     const int smem = 3 * kBins * (int)sizeof(uint32_t);
-    if (!attr_set) {
-        if (cudaFuncSetAttribute(k_awb_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, smem) != cudaSuccess)
-            return -5;
-        attr_set = true;
-    }
+    if (craw_smem_attr(k_awb_reduce, (size_t)smem, attr_done) < 0)
+        return -5;
     /* About 4096 records a CTA, at most one CTA an SM of a 152-SM part. */
     uint32_t grid = (n + 4095) / 4096;
     grid = grid < 1 ? 1 : (grid > 148 ? 148 : grid);

@@ -7,9 +7,30 @@
 #include <cuda_fp16.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "../kabi.h"
 
 #define CRAW_DEV __device__ __forceinline__
+
+/* Lets `fn` take `bytes` of dynamic shared memory, once per device (the
+ * attribute belongs to the function in each device's context); `done`
+ * holds a bit per device ordinal below 64, above which it is set every
+ * time. 0, or -5 when the runtime refuses. */
+template <typename F>
+inline int craw_smem_attr(F fn, size_t bytes, std::atomic<uint64_t> &done)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return -5;
+    const uint64_t bit = dev >= 0 && dev < 64 ? (uint64_t)1 << dev : 0;
+    if (bit && (done.load(std::memory_order_acquire) & bit))
+        return 0;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+        return -5;
+    done.fetch_or(bit, std::memory_order_release);
+    return 0;
+}
 
 /* Mirror without repeating the edge sample (reference common.glsl:49-55,
  * lib/ref/ref_debayer.c:21-34), looping for tiles that hang further past

@@ -25,12 +25,9 @@ int launch(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, cudaStream_t s)
     using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2>;
     auto fn = k_denoise<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2>;
     const size_t smem = (size_t)C::smem_floats * sizeof(float);
-    static bool attr_set = false;   /* per process; the attribute is per function */
-    if (!attr_set) {
-        if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
-            return -5;
-        attr_set = true;
-    }
+    static std::atomic<uint64_t> attr_done{ 0 };
+    if (craw_smem_attr(fn, smem, attr_done) < 0)
+        return -5;
     dim3 grid((k->pw + C::OX - 1) / C::OX, (k->ph + C::OY - 1) / C::OY);
     fn<<<grid, C::NT, smem, s>>>(*k, *io);
     return cudaGetLastError() == cudaSuccess ? 0 : -5;

@@ -153,21 +153,21 @@ typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, 
 
 bool mosaic_tmap(const void *src, size_t pitch, int w, int h, CUtensorMap *out)
 {
-    static EncodeTiled encode = nullptr;
-    static bool looked = false;
+    /* Looked up once per process (a thread-safe static initialisation). */
+    static const EncodeTiled encode = [] {
+        void *fn = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        EncodeTiled e = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess && q == cudaDriverEntryPointSuccess)
+            e = reinterpret_cast<EncodeTiled>(fn);
+        (void)cudaGetLastError();
+        return e;
+    }();
     thread_local const void *c_src = nullptr;
     thread_local size_t c_pitch = 0;
     thread_local int c_w = 0, c_h = 0;
     thread_local CUtensorMap c_map;
-    if (!looked) {
-        void *fn = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess && q == cudaDriverEntryPointSuccess)
-            encode = reinterpret_cast<EncodeTiled>(fn);
-        (void)cudaGetLastError();
-        looked = true;
-    }
     if (!encode || ((uintptr_t)src & 15) || (pitch & 15))
         return false;
     if (src != c_src || pitch != c_pitch || w != c_w || h != c_h) {
@@ -227,15 +227,10 @@ int launch(const CRAWKDevelop *k, const CRAWKDevelopIO *io, cudaStream_t s)
 int launch_rcd(const CRAWKDevelop *k, const CRAWKDevelopIO *io, cudaStream_t s)
 {
     constexpr size_t smem = RcdQuads<QTW, QTH, QNT>::floats * sizeof(float);
-    static bool attr_set = false;
-    if (!attr_set) {
-        if (cudaFuncSetAttribute(k_develop_rcd_quads, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem) != cudaSuccess ||
-            cudaFuncSetAttribute(k_develop_rcd_quads_tma, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)smem) != cudaSuccess)
-            return -5;
-        attr_set = true;
-    }
+    static std::atomic<uint64_t> attr_plain{ 0 }, attr_tma{ 0 };
+    if (craw_smem_attr(k_develop_rcd_quads, smem, attr_plain) < 0 ||
+        craw_smem_attr(k_develop_rcd_quads_tma, smem, attr_tma) < 0)
+        return -5;
     QuadGrid g;
     g.init(k->width, k->height);
     if (g.interior_x() > 0 && g.interior_y() > 0) {
