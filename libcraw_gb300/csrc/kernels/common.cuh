@@ -77,17 +77,11 @@ CRAW_DEV f2x f2_pack(float lo, float hi)
 }
 CRAW_DEV float f2_lo(f2x a)
 {
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a));
-    (void)hi;
-    return lo;
+    return __uint_as_float((uint32_t)a);
 }
 CRAW_DEV float f2_hi(f2x a)
 {
-    float lo, hi;
-    asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a));
-    (void)lo;
-    return hi;
+    return __uint_as_float((uint32_t)(a >> 32));
 }
 CRAW_DEV f2x f2_add(f2x a, f2x b)
 {

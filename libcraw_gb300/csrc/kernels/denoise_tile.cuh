@@ -59,12 +59,25 @@ CRAW_DEV float level(const CRAWKDenoise &k, uint32_t raw, int pl)
 }
 
 /* The four plane samples of mosaic quad (qx, qy): R, Gr, Gb, B. */
-CRAW_DEV void load_quad_u16(const CRAWKDenoiseIO &io, int qx, int qy, uint32_t q[4])
+/* The quad at plane position (qx, qy): its two mosaic rows as 32-bit
+ * pairs (a: R, Gr; b: Gb, B) and the four samples. */
+CRAW_DEV void load_quad_u16(const CRAWKDenoiseIO &io, int qx, int qy, uint32_t q[4], uint32_t &a, uint32_t &b)
 {
     const char *r0 = (const char *)io.src + (size_t)(2 * qy) * io.src_pitch;
-    uint32_t a = __ldg(reinterpret_cast<const uint32_t *>(r0) + qx);
-    uint32_t b = __ldg(reinterpret_cast<const uint32_t *>(r0 + io.src_pitch) + qx);
+    a = __ldg(reinterpret_cast<const uint32_t *>(r0) + qx);
+    b = __ldg(reinterpret_cast<const uint32_t *>(r0 + io.src_pitch) + qx);
     q[0] = a & 0xffffu; q[1] = a >> 16; q[2] = b & 0xffffu; q[3] = b >> 16;
+}
+
+/* Keeps the raw rows of a quad of the tile's own region (plane position
+ * (cc, cr) within it) in the RW_W-wide raw array. */
+template <int OX, int OY>
+CRAW_DEV void keep_raw(uint32_t *rw, int cr, int cc, uint32_t a, uint32_t b)
+{
+    if (cr >= 0 && cr < OY && cc >= 0 && cc < OX) {
+        rw[(2 * cr) * OX + cc] = a;
+        rw[(2 * cr + 1) * OX + cc] = b;
+    }
 }
 
 CRAW_DEV void load_quad_f32(const float *base, size_t pitch, int qx, int qy, float q[4])
@@ -91,8 +104,15 @@ struct Cfg {
     static constexpr bool PACKED = X2 && SPATIAL;
     static constexpr int TO_OFF = HISTORY ? 8 * TN + 8 * EN : 4 * TN;
     static constexpr int VO_OFF = TO_OFF + 4 * TN;
-    static constexpr int smem_floats = 4 * TN * (HISTORY ? 2 : 1) + (HISTORY ? 8 * EN : 0) +
+    static constexpr int BASE_FLOATS = 4 * TN * (HISTORY ? 2 : 1) + (HISTORY ? 8 * EN : 0) +
                                        (PACKED ? 4 * TN * (HISTORY ? 2 : 1) : 0);
+    /* The tile's own mosaic region, 2 OX x 2 OY 16-bit samples: the raw
+     * samples the fill read (for the highlight guard), then the denoised
+     * output until it is stored as whole 16-byte rows. */
+    static constexpr int RW_W = 2 * OX, RW_H = 2 * OY;
+    static constexpr int RW_OFF = BASE_FLOATS;
+    static_assert(RW_OFF % 4 == 0 && RW_W % 8 == 0, "16-byte rows");
+    static constexpr int smem_floats = BASE_FLOATS + RW_W * RW_H / 2;
 };
 
 /* The NLM search of one thread: BW columns x M rows of one plane, at the
@@ -333,12 +353,14 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
 
     /* ---- fill: the stabilised tile, temporally averaged when there is a
      * history (reference lib/ref/ref_denoise.c:244-296). */
+    uint32_t *raw32 = reinterpret_cast<uint32_t *>(smem + C::RW_OFF);
     if constexpr (!HISTORY) {
         for (int i = tid; i < TX * TY; i += NT) {
             int r = i / TX, c = i % TX;
             int qy = craw_mirror(ty0 - R + r, k.ph), qx = craw_mirror(tx0 - R + c, k.pw);
-            uint32_t q[4];
-            load_quad_u16(io, qx, qy, q);
+            uint32_t q[4], qa, qb;
+            load_quad_u16(io, qx, qy, q, qa, qb);
+            keep_raw<OX, OY>(raw32, r - R, c - R, qa, qb);
 #pragma unroll
             for (int pl = 0; pl < 4; pl++) {
                 const float t = gat_fwd(k, level(k, q[pl], pl));
@@ -352,9 +374,10 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
         for (int i = tid; i < C::EN; i += NT) {
             int r = i / C::EX, c = i % C::EX;
             int qy = craw_mirror(ty0 - R - 1 + r, k.ph), qx = craw_mirror(tx0 - R - 1 + c, k.pw);
-            uint32_t q[4];
+            uint32_t q[4], qa, qb;
             float lp[4];
-            load_quad_u16(io, qx, qy, q);
+            load_quad_u16(io, qx, qy, q, qa, qb);
+            keep_raw<OX, OY>(raw32, r - R - 1, c - R - 1, qa, qb);
             load_quad_f32(io.lvl_prev, io.lvl_pitch, qx, qy, lp);
 #pragma unroll
             for (int pl = 0; pl < 4; pl++) {
@@ -464,13 +487,36 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
                 }
             }
             float u = gat_inv(k, SPATIAL ? res[m][j] : tc);
-            uint16_t raw0 = __ldg((const uint16_t *)((const char *)io.src + (size_t)my * io.src_pitch) + mx);
+            /* The sample's raw value, kept by the fill, and in its place
+             * the output. */
+            uint16_t *cell = reinterpret_cast<uint16_t *>(raw32) + (2 * (oy0 + m) + py) * C::RW_W +
+                             2 * (ox0 + j) + px;
+            const uint16_t raw0 = *cell;
             float u0 = ((float)raw0 * (1.0f / 65535.0f) - blk) * irng;
             float gr = fminf(fmaxf((u0 - k.guard_lo) * k.guard_inv, 0.0f), 1.0f);
             u = u + (u0 - u) * gr;
             float ro = fminf(fmaxf(blk + u * rng, 0.0f), 1.0f);
-            uint16_t *dr = (uint16_t *)((char *)io.dst + (size_t)my * io.dst_pitch);
-            dr[mx] = (uint16_t)rintf(ro * 65535.0f);
+            *cell = (uint16_t)rintf(ro * 65535.0f);
+        }
+    }
+
+    /* The tile's mosaic region out, 16 bytes a thread (element by element
+     * at the frame's right edge, or if the rows are not 16-byte aligned). */
+    __syncthreads();
+    constexpr int CH = C::RW_W / 8;
+    const int mx0 = 2 * tx0, my0 = 2 * ty0, W = 2 * k.pw, H = 2 * k.ph;
+    const bool a16 = !(((uintptr_t)io.dst | io.dst_pitch) & 15);
+    const uint16_t *raw16 = reinterpret_cast<const uint16_t *>(raw32);
+    for (int i = tid; i < C::RW_H * CH; i += NT) {
+        const int yy = i / CH, xx = (i % CH) * 8, my = my0 + yy, mx = mx0 + xx;
+        if (my >= H || mx >= W)
+            continue;
+        uint16_t *dr = (uint16_t *)((char *)io.dst + (size_t)my * io.dst_pitch) + mx;
+        if (a16 && mx + 8 <= W) {
+            *reinterpret_cast<uint4 *>(dr) = reinterpret_cast<const uint4 *>(raw32)[i];
+        } else {
+            for (int e = 0; e < 8 && mx + e < W; e++)
+                dr[e] = raw16[yy * C::RW_W + xx + e];
         }
     }
 }
