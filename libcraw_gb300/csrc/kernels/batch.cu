@@ -31,7 +31,7 @@ constexpr int BQH = 16;     /* rows of a develop item (a 64 x 16 quad tile) */
 /* The denoise of a batch: the packed f32x2 search, 2 columns x M rows a
  * thread, 256 threads. */
 template <int M> struct DnShape {
-    using C = craw_dn::Cfg<2, M, 2, true, false, false, true>;
+    using C = craw_dn::Cfg<2, M, 2, true, false, false, true, false>;
 };
 
 /* The frame an item of a phase belongs to: the last one whose first item
@@ -52,8 +52,8 @@ CRAW_DEV void denoise_phase(const CRAWKBatchTable &T, int nb, int items, float *
         const CRAWKBatchFrame &F = T.f[item_frame(T, nb, it, false)];
         const int local = it - F.dn_first;
         __syncthreads();   /* the previous item's shared memory is free */
-        craw_dn::denoise_tile<2, M, 2, true, false, false, true>(F.dn, F.dio, local % F.dn_tx,
-                                                           local / F.dn_tx, smem);
+        craw_dn::denoise_tile<2, M, 2, true, false, false, true, false>(F.dn, F.dio, local % F.dn_tx,
+                                                                  local / F.dn_tx, smem);
     }
 }
 
@@ -107,8 +107,10 @@ k_batch_denoise(const __grid_constant__ CRAWKBatchTable T, int nb, int dn_items,
     denoise_phase<M>(T, nb, dn_items, smem);
 }
 
+/* Four CTAs an SM, the shared memory's limit for RCD items: registers
+ * kept at 64 a thread so that they do not set a lower one. */
 template <int METHOD>
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, 4)
 k_batch_develop(const __grid_constant__ CRAWKBatchTable T, int nb, int dn_items, int dv_items)
 {
     extern __shared__ __align__(16) float smem[];

@@ -88,7 +88,10 @@ CRAW_DEV void load_quad_f32(const float *base, size_t pitch, int qx, int qy, flo
     q[0] = a.x; q[1] = a.y; q[2] = b.x; q[3] = b.y;
 }
 
-template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2 = false>
+/* STAGED: the tile's raw mosaic and its output pass through shared memory
+ * (below); the batch's persistent kernel leaves it off, whose shared
+ * memory would otherwise cost it a CTA an SM. */
+template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2 = false, bool STAGED = true>
 struct Cfg {
     static constexpr int R = SPATIAL ? S + P : 0;       /* apron of the tile */
     static constexpr int OX = 16 * BW, OY = 2 * M * WP;  /* plane samples per tile */
@@ -112,7 +115,7 @@ struct Cfg {
     static constexpr int RW_W = 2 * OX, RW_H = 2 * OY;
     static constexpr int RW_OFF = BASE_FLOATS;
     static_assert(RW_OFF % 4 == 0 && RW_W % 8 == 0, "16-byte rows");
-    static constexpr int smem_floats = BASE_FLOATS + RW_W * RW_H / 2;
+    static constexpr int smem_floats = BASE_FLOATS + (STAGED ? RW_W * RW_H / 2 : 0);
 };
 
 /* The NLM search of one thread: BW columns x M rows of one plane, at the
@@ -336,10 +339,10 @@ struct SearchX2 {
 
 /* One tile (tile column bx, tile row by) of all four planes; the whole
  * CTA takes part. `smem` holds Cfg::smem_floats floats. */
-template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2 = false>
+template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2 = false, bool STAGED = true>
 CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int bx, int by, float *smem)
 {
-    using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2>;
+    using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2, STAGED>;
     static_assert(!C::PACKED || BW == 2, "the packed search pairs a thread's two columns");
     constexpr int R = C::R, OX = C::OX, OY = C::OY, TX = C::TX, TY = C::TY, TS = C::TS;
     constexpr int NT = C::NT;
@@ -360,7 +363,8 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
             int qy = craw_mirror(ty0 - R + r, k.ph), qx = craw_mirror(tx0 - R + c, k.pw);
             uint32_t q[4], qa, qb;
             load_quad_u16(io, qx, qy, q, qa, qb);
-            keep_raw<OX, OY>(raw32, r - R, c - R, qa, qb);
+            if constexpr (STAGED)
+                keep_raw<OX, OY>(raw32, r - R, c - R, qa, qb);
 #pragma unroll
             for (int pl = 0; pl < 4; pl++) {
                 const float t = gat_fwd(k, level(k, q[pl], pl));
@@ -377,7 +381,8 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
             uint32_t q[4], qa, qb;
             float lp[4];
             load_quad_u16(io, qx, qy, q, qa, qb);
-            keep_raw<OX, OY>(raw32, r - R - 1, c - R - 1, qa, qb);
+            if constexpr (STAGED)
+                keep_raw<OX, OY>(raw32, r - R - 1, c - R - 1, qa, qb);
             load_quad_f32(io.lvl_prev, io.lvl_pitch, qx, qy, lp);
 #pragma unroll
             for (int pl = 0; pl < 4; pl++) {
@@ -487,18 +492,28 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
                 }
             }
             float u = gat_inv(k, SPATIAL ? res[m][j] : tc);
-            /* The sample's raw value, kept by the fill, and in its place
-             * the output. */
+            /* The sample's raw value (kept by the fill when STAGED), and in
+             * its place the output. */
             uint16_t *cell = reinterpret_cast<uint16_t *>(raw32) + (2 * (oy0 + m) + py) * C::RW_W +
                              2 * (ox0 + j) + px;
-            const uint16_t raw0 = *cell;
+            uint16_t raw0;
+            if constexpr (STAGED)
+                raw0 = *cell;
+            else
+                raw0 = __ldg((const uint16_t *)((const char *)io.src + (size_t)my * io.src_pitch) + mx);
             float u0 = ((float)raw0 * (1.0f / 65535.0f) - blk) * irng;
             float gr = fminf(fmaxf((u0 - k.guard_lo) * k.guard_inv, 0.0f), 1.0f);
             u = u + (u0 - u) * gr;
             float ro = fminf(fmaxf(blk + u * rng, 0.0f), 1.0f);
-            *cell = (uint16_t)rintf(ro * 65535.0f);
+            const uint16_t code = (uint16_t)rintf(ro * 65535.0f);
+            if constexpr (STAGED)
+                *cell = code;
+            else
+                ((uint16_t *)((char *)io.dst + (size_t)my * io.dst_pitch))[mx] = code;
         }
     }
+    if constexpr (!STAGED)
+        return;
 
     /* The tile's mosaic region out, 16 bytes a thread (element by element
      * at the frame's right edge, or if the rows are not 16-byte aligned). */
