@@ -45,6 +45,8 @@ import numpy as np  # noqa: E402
 
 METRIC = "5760x3240 frames/s full develop; p50/p99 frame latency at <=1e-3 rel err"
 WORKLOAD = "5760x3240 RGGB 12-bit: VST + NLM 1.0 + RCD + ACES AP1 (RGC) float32 + AWB histogram"
+#: Pipelines the end-to-end leg rotates over (`--e2e-lanes`).
+E2E_LANES = 3
 #: Denoise tile shapes by craw_pipeline_get_kernel_config() index.
 DN_SHAPES = ["2x8", "2x4", "2x8 f32x2", "2x4 f32x2"]
 #: dram__bytes_read.sum + dram__bytes_write.sum of one launch of the stage's
@@ -68,6 +70,8 @@ def parse():
                          "noise, cpu")
     ap.add_argument("--force-shape", type=int, default=-1,
                     help="denoise tile shape index instead of the autotuner's (profiling)")
+    ap.add_argument("--e2e-lanes", type=int, default=0,
+                    help="pipelines the end-to-end leg rotates over (0: the default)")
     ap.add_argument("--width", type=int, default=5760)
     ap.add_argument("--height", type=int, default=3240)
     return ap.parse_args()
@@ -268,6 +272,9 @@ def run_reference(args):
 def run_gpu(args):
     import torch
 
+    global E2E_LANES
+    if args.e2e_lanes > 0:
+        E2E_LANES = args.e2e_lanes
     rank, ws, local = dist_init()
     import libcraw_gb300 as L
     from libcraw_gb300 import build as B
@@ -375,12 +382,12 @@ def run_gpu(args):
                                "peak = SMs x 128 FP32 lanes x median SM clock"}
 
     # End to end through the same call: pinned host mosaic in, RGBA32F out.
-    # Three lanes (pipeline + CUDA stream + device buffers each) take the
-    # steps in turn, so one frame's copy in, another's kernels and a third's
-    # copy out overlap, as a caller streaming frames would arrange it.
+    # E2E_LANES lanes (pipeline + CUDA stream + device buffers each) take
+    # the steps in turn, so one frame's copy in, another's kernels and
+    # others' copies out overlap, as a caller streaming frames would.
     pinned_in = [torch.from_numpy(f.view(np.int16)).pin_memory() for f in host_frames]
     lanes = []
-    for _ in range(3):
+    for _ in range(E2E_LANES):
         ls = torch.cuda.Stream()
         d_in = torch.empty((h, w), dtype=torch.int16, device="cuda")
         d_out = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
@@ -414,7 +421,7 @@ def run_gpu(args):
            "d2h_bytes_per_step": w * h * 16,
            "one_stream_value": ws * args.steps / e2e_s1,
            "how": "per step: H2D of the mosaic from pinned memory, craw_pipeline_record, D2H of "
-                  "the RGBA32F frame to pinned memory, on one of 3 streams in turn (each with its "
+                  f"the RGBA32F frame to pinned memory, on one of {E2E_LANES} streams in turn (each with its "
                   "own pipeline and buffers); wall clock over all steps; one_stream_value: all "
                   "steps on one stream"}
     for ln in lanes:
