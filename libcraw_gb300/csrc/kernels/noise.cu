@@ -17,8 +17,8 @@
  *
  * The median is an order statistic, so it is the reference's value
  * exactly; so are the counts. A bin's sum of means is kept as an integer
- * (each float mean times 2^64, exact for means >= 2^-40, in two 32-bit
- * halves) so that it does not depend on the order the atomics land in;
+ * (each float mean times 2^64, exact for means >= 2^-40, in three 32-bit
+ * words) so that it does not depend on the order the atomics land in;
  * the reference adds the same floats into a double one by one. Built
  * without multiply-add contraction, as the reference's host code is.
  */
