@@ -123,13 +123,16 @@ struct Cfg {
  * lib/ref/ref_denoise.c:109-154). Weights as exp2 on the MUFU:
  * exp(-max(d2/(9h^2) - 2, 0)) = 2^min(d2 * c1 + c0, 0) with
  * c1 = -log2(e)/(9h^2), c0 = 2 log2(e); with a history
- * exp(-max(d2/(9h^2) - (vc + vq), 0) / vc) = 2^min((vc + vq - d2/(9h^2)) * log2(e)/vc, 0). */
+ * exp(-max(d2/(9h^2) - (vc + vq), 0) / vc) = 2^min((vc + vq - d2/(9h^2)) * log2(e)/vc, 0),
+ * expanded as 2^min(log2(e) + vq * lvc + d2 * nkl, 0) with the centre's
+ * lvc = log2(e)/vc and nkl = -lvc/(9h^2) taken out of the search: two
+ * multiply-adds an offset. */
 template <int BW, int M, int R, int TS, bool HISTORY>
 struct Search {
     static_assert(BW % 2 == 0 && M % 2 == 0, "pairs of columns and rows");
     float own[M + 2][BW + 2];
     float acc[M][BW], wsum[M][BW];
-    float vc[HISTORY ? M : 1][BW], lvc[HISTORY ? M : 1][BW];
+    float nkl[HISTORY ? M : 1][BW], lvc[HISTORY ? M : 1][BW];
     float kd, c1, c0;
 
     CRAW_DEV void init(const float *Tp, const float *Vp, int ox0, int oy0, float inv_h2)
@@ -149,8 +152,8 @@ struct Search {
                 acc[m][j] = 0.0f;
                 wsum[m][j] = 0.0f;
                 if constexpr (HISTORY) {
-                    vc[m][j] = Vp[(oy0 + R + m) * TS + ox0 + R + j];
-                    lvc[m][j] = __fdiv_rn(kLog2e, vc[m][j]);
+                    lvc[m][j] = __fdiv_rn(kLog2e, Vp[(oy0 + R + m) * TS + ox0 + R + j]);
+                    nkl[m][j] = -kd * lvc[m][j];
                 }
             }
     }
@@ -217,8 +220,9 @@ struct Search {
                     float d2a = hs[m][j] + mid, d2b = mid + hs[m + 3][j];
                     float wa, wb;
                     if constexpr (HISTORY) {
-                        wa = craw_ex2(fminf(fmaf(d2a, -kd, vc[m][j] + vq[m][j + 1 + dx + S]) * lvc[m][j], 0.0f));
-                        wb = craw_ex2(fminf(fmaf(d2b, -kd, vc[m + 1][j] + vq[m + 1][j + 1 + dx + S]) * lvc[m + 1][j], 0.0f));
+                        wa = craw_ex2(fminf(fmaf(d2a, nkl[m][j], fmaf(vq[m][j + 1 + dx + S], lvc[m][j], kLog2e)), 0.0f));
+                        wb = craw_ex2(fminf(fmaf(d2b, nkl[m + 1][j],
+                                                 fmaf(vq[m + 1][j + 1 + dx + S], lvc[m + 1][j], kLog2e)), 0.0f));
                     } else {
                         wa = craw_ex2(fminf(fmaf(d2a, c1, c0), 0.0f));
                         wb = craw_ex2(fminf(fmaf(d2b, c1, c0), 0.0f));
@@ -247,8 +251,8 @@ struct SearchX2 {
     static_assert(R - 1 == S, "window origin");
     f2x own[M + 2][2];            /* columns (0,1), (2,3) of the patch block */
     f2x acc[M], wsum[M];
-    f2x vc[HISTORY ? M : 1], lvc[HISTORY ? M : 1];
-    f2x c1, c0, nkd;
+    f2x nkl[HISTORY ? M : 1], lvc[HISTORY ? M : 1];
+    f2x c1, c0;
 
     CRAW_DEV void init(const float *To, const float *Vp, int ox0, int oy0, float inv_h2)
     {
@@ -262,15 +266,17 @@ struct SearchX2 {
         }
         const float kd = (1.0f / 9.0f) * inv_h2;
         c1 = f2_pack(-kLog2e * kd, -kLog2e * kd);
-        c0 = f2_pack(2.0f * kLog2e, 2.0f * kLog2e);
-        nkd = f2_pack(-kd, -kd);
+        /* With a history the constant term is log2(e) (Search's expansion). */
+        c0 = HISTORY ? f2_pack(kLog2e, kLog2e) : f2_pack(2.0f * kLog2e, 2.0f * kLog2e);
 #pragma unroll
         for (int m = 0; m < M; m++) {
             acc[m] = wsum[m] = f2_pack(0.0f, 0.0f);
             if constexpr (HISTORY) {
                 /* The centres' variance: columns ox0 + R, + R + 1 (aligned). */
-                vc[m] = f2_ld(Vp + (oy0 + R + m) * TS + ox0 + R);
-                lvc[m] = f2_pack(__fdiv_rn(kLog2e, f2_lo(vc[m])), __fdiv_rn(kLog2e, f2_hi(vc[m])));
+                const f2x vc = f2_ld(Vp + (oy0 + R + m) * TS + ox0 + R);
+                const float l0 = __fdiv_rn(kLog2e, f2_lo(vc)), l1 = __fdiv_rn(kLog2e, f2_hi(vc));
+                lvc[m] = f2_pack(l0, l1);
+                nkl[m] = f2_pack(-kd * l0, -kd * l1);
             }
         }
     }
@@ -317,8 +323,8 @@ struct SearchX2 {
                     const float *vsrc = (o & 1) ? Vp : Vo;
                     const f2x vqa = f2_ld(vsrc + (oy0 + R + dy + m) * TS + vcol);
                     const f2x vqb = f2_ld(vsrc + (oy0 + R + dy + m + 1) * TS + vcol);
-                    xa = f2_mul(f2_fma(d2a, nkd, f2_add(vc[m], vqa)), lvc[m]);
-                    xb = f2_mul(f2_fma(d2b, nkd, f2_add(vc[m + 1], vqb)), lvc[m + 1]);
+                    xa = f2_fma(d2a, nkl[m], f2_fma(vqa, lvc[m], c0));
+                    xb = f2_fma(d2b, nkl[m + 1], f2_fma(vqb, lvc[m + 1], c0));
                 } else {
                     xa = f2_fma(d2a, c1, c0);
                     xb = f2_fma(d2b, c1, c0);
