@@ -194,10 +194,12 @@ def whole_job_rate(units_per_rank: int, ws: int, seconds_per_rank: float) -> flo
 
 # ------------------------------------------------------------- CPU baseline
 
-def cpu_oracle_fps(frame: np.ndarray, params, fp, rows_frac: float = 0.25) -> dict:
+def cpu_oracle_fps(frame: np.ndarray, params, fp, rows_frac: float = 0.25, single: bool = True) -> dict:
     """The CPU oracle (float restatement of the reference's lib/ref) on
     `rows_frac` of a frame, split into one strip per host thread, each strip
-    developed as a frame of its own: frames/s = rows_frac / wall time."""
+    developed as a frame of its own: frames/s = rows_frac / wall time.
+    `single`: also time one strip alone on one thread (outside that wall
+    time) for the single-threaded milliseconds a frame."""
     sys.path.insert(0, str(ROOT / "tests"))
     from oracle import Oracle
     import libcraw_gb300 as L
@@ -222,9 +224,35 @@ def cpu_oracle_fps(frame: np.ndarray, params, fp, rows_frac: float = 0.25) -> di
         t.join()
     dt = time.perf_counter() - t0
     done = rows * cores / h
-    return {"value": done / dt, "unit": "frames/s", "cores": cores, "kind": "port",
-            "sample": f"{cores} strips of {w}x{rows} ({done:.3f} of a frame) through the float "
-                      f"oracle (lib/ref restated), one strip per host thread, {dt:.2f} s wall"}
+    res = {"value": done / dt, "unit": "frames/s", "cores": cores, "kind": "port",
+           "sample": f"{cores} strips of {w}x{rows} ({done:.3f} of a frame) through the float "
+                     f"oracle (lib/ref restated), one strip per host thread, {dt:.2f} s wall",
+           "nproc": cores, "cpu_model": cpu_model()}
+    if single:
+        t1 = time.perf_counter()
+        work(0)
+        res["single_thread_ms_per_frame"] = (time.perf_counter() - t1) * 1e3 * h / rows
+    return res
+
+
+def cpu_model() -> str:
+    """The host CPU's name as /proc/cpuinfo gives it (x86: "model name";
+    Arm: implementer and part numbers), else the machine type."""
+    import platform
+    try:
+        info = open("/proc/cpuinfo").read().splitlines()
+    except OSError:
+        return platform.machine()
+    fields = {}
+    for line in info:
+        k, _, v = line.partition(":")
+        fields.setdefault(k.strip(), v.strip())
+    if "model name" in fields:
+        return fields["model name"]
+    if "CPU part" in fields:
+        return (f"{platform.machine()} implementer {fields.get('CPU implementer', '?')} "
+                f"part {fields['CPU part']}")
+    return platform.machine()
 
 
 def run_reference(args):
@@ -244,11 +272,11 @@ def run_reference(args):
     fp = L.frame_params(prof, **c.frame_kwargs())
     frac = 0.5
     for _ in range(args.warmup):
-        cpu_oracle_fps(frame, pp, fp, frac)
+        cpu_oracle_fps(frame, pp, fp, frac, single=False)
     times = []
     last = None
-    for _ in range(args.steps):
-        last = cpu_oracle_fps(frame, pp, fp, frac)
+    for i in range(args.steps):
+        last = cpu_oracle_fps(frame, pp, fp, frac, single=i == args.steps - 1)
         times.append(frac / last["value"])
     total = sum(times)
     value = args.steps * frac / total
