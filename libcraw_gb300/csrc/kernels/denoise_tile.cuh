@@ -103,7 +103,10 @@ struct Cfg {
     static constexpr int NT = 4 * WP * 32;
     /* The packed search (X2) keeps copies of the tile (and, with a
      * history, of the variance) shifted left by one sample, so that odd
-     * column pairs load as aligned float2: TO and VO, after the rest. */
+     * column pairs load as aligned float2: TO and VO, after the rest.
+     * (Placing them over the history's ring arrays, dead once the temporal
+     * average is done, needs a separate copy pass after a barrier; at
+     * 5760x3240 that cost more than the third CTA an SM it allows.) */
     static constexpr bool PACKED = X2 && SPATIAL;
     static constexpr int TO_OFF = HISTORY ? 8 * TN + 8 * EN : 4 * TN;
     static constexpr int VO_OFF = TO_OFF + 4 * TN;
