@@ -408,6 +408,13 @@ def run_gpu(args):
                       "frac": ops / peak_lane_ops,
                       "model": "N*49*13 FP32 lane-ops per frame (7x7 search, 13 ops an offset); "
                                "peak = SMs x 128 FP32 lanes x median SM clock"}
+            # The HBM fraction is small by nature: the NLM does 637 FP32
+            # operations per 4 bytes moved. The binding roofline is the FP32 pipe.
+            roof["binding"] = "fp32"
+            roof["binding_frac"] = roof32["frac"]
+            roof["note"] = ("the denoise is bound by the FP32 pipe, not by HBM: "
+                            f"{roof32['frac']:.2f} of the FP32 lane rate (roofline_fp32), "
+                            f"{roof['frac']:.3f} of HBM")
 
     # End to end through the same call: pinned host mosaic in, RGBA32F out.
     # E2E_LANES lanes (pipeline + CUDA stream + device buffers each) take
