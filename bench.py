@@ -250,6 +250,12 @@ def cpu_model() -> str:
     if "model name" in fields:
         return fields["model name"]
     if "CPU part" in fields:
+        # Arm Ltd (implementer 0x41) cores by part number.
+        arm = {"0xd0c": "Neoverse-N1", "0xd40": "Neoverse-V1", "0xd49": "Neoverse-N2",
+               "0xd4f": "Neoverse-V2", "0xd84": "Neoverse-V3"}
+        part = fields["CPU part"].lower()
+        if fields.get("CPU implementer", "").lower() == "0x41" and part in arm:
+            return f"Arm {arm[part]}"
         return (f"{platform.machine()} implementer {fields.get('CPU implementer', '?')} "
                 f"part {fields['CPU part']}")
     return platform.machine()
