@@ -400,37 +400,56 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
             }
         }
         __syncthreads();
-        for (int i = tid; i < TX * TY; i += NT) {
-            int r = i / TX, c = i % TX;
-            int qy = craw_mirror(ty0 - R + r, k.ph), qx = craw_mirror(tx0 - R + c, k.pw);
-            const char *vr = (const char *)io.var_prev + (size_t)(2 * qy) * io.var_pitch;
-            uint16_t v0 = __ldg(reinterpret_cast<const uint16_t *>(vr) + qx);
-            uint16_t v1 = __ldg(reinterpret_cast<const uint16_t *>(vr + io.var_pitch) + qx);
-            uint32_t sv[4] = { v0 & 0xffu, (uint32_t)v0 >> 8, v1 & 0xffu, (uint32_t)v1 >> 8 };
+        /* A thread takes KR rows of one column, so that the 3x3 sums of
+         * squared differences share their row sums: KR + 2 row sums of
+         * three, then KR column sums of three (the same nine terms as the
+         * reference's row-major sum, added in another order). */
+        constexpr int KR = 4;
+        static_assert(TY % KR == 0, "whole runs of rows");
+        for (int i = tid; i < TX * (TY / KR); i += NT) {
+            const int c = i % TX, r0 = (i / TX) * KR;
+            const int qx = craw_mirror(tx0 - R + c, k.pw);
+            uint32_t sv[KR][4];
+#pragma unroll
+            for (int j = 0; j < KR; j++) {
+                const int qy = craw_mirror(ty0 - R + r0 + j, k.ph);
+                const char *vr = (const char *)io.var_prev + (size_t)(2 * qy) * io.var_pitch;
+                const uint16_t v0 = __ldg(reinterpret_cast<const uint16_t *>(vr) + qx);
+                const uint16_t v1 = __ldg(reinterpret_cast<const uint16_t *>(vr + io.var_pitch) + qx);
+                sv[j][0] = v0 & 0xffu;
+                sv[j][1] = (uint32_t)v0 >> 8;
+                sv[j][2] = v1 & 0xffu;
+                sv[j][3] = (uint32_t)v1 >> 8;
+            }
 #pragma unroll
             for (int pl = 0; pl < 4; pl++) {
                 const float *cp = TC + pl * C::EN, *pp = TPv + pl * C::EN;
-                int e0 = (r + 1) * C::EX + c + 1;
-                float d2 = 0.0f;
+                /* Ring rows r0 .. r0 + KR + 1, columns c .. c + 2: the 3x3
+                 * windows of tile rows r0 .. r0 + KR - 1 at column c. */
+                float hs[KR + 2];
 #pragma unroll
-                for (int ky = -1; ky <= 1; ky++)
+                for (int j = 0; j < KR + 2; j++) {
+                    const int e = (r0 + j) * C::EX + c;
+                    const float a0 = pp[e] - cp[e], a1 = pp[e + 1] - cp[e + 1], a2 = pp[e + 2] - cp[e + 2];
+                    hs[j] = __fadd_rn(__fadd_rn(__fmul_rn(a0, a0), __fmul_rn(a1, a1)), __fmul_rn(a2, a2));
+                }
 #pragma unroll
-                    for (int kx = -1; kx <= 1; kx++) {
-                        float e = pp[e0 + ky * C::EX + kx] - cp[e0 + ky * C::EX + kx];
-                        d2 = __fadd_rn(d2, __fmul_rn(e, e));
-                    }
-                float x = d2 * (1.0f / 9.0f) * k.t_inv_h2 - 2.0f;
-                float a = k.t_alpha * expf(-fmaxf(x, 0.0f));
-                float sp = (float)sv[pl] * (1.0f / 255.0f);
-                float vv = __fadd_rn(__fmul_rn(1.0f - a, 1.0f - a), __fmul_rn(a * a, sp * sp));
-                const float t = __fadd_rn(__fmul_rn(cp[e0], 1.0f - a), __fmul_rn(pp[e0], a));
-                T[pl * C::TN + r * TS + c] = t;
-                V[pl * C::TN + r * TS + c] = fmaxf(vv, kVarMin);
-                if constexpr (C::PACKED)
-                    if (c > 0) {
-                        smem[C::TO_OFF + pl * C::TN + r * TS + c - 1] = t;
-                        smem[C::VO_OFF + pl * C::TN + r * TS + c - 1] = fmaxf(vv, kVarMin);
-                    }
+                for (int j = 0; j < KR; j++) {
+                    const int r = r0 + j, e0 = (r + 1) * C::EX + c + 1;
+                    const float d2 = __fadd_rn(__fadd_rn(hs[j], hs[j + 1]), hs[j + 2]);
+                    float x = d2 * (1.0f / 9.0f) * k.t_inv_h2 - 2.0f;
+                    float a = k.t_alpha * expf(-fmaxf(x, 0.0f));
+                    float sp = (float)sv[j][pl] * (1.0f / 255.0f);
+                    float vv = __fadd_rn(__fmul_rn(1.0f - a, 1.0f - a), __fmul_rn(a * a, sp * sp));
+                    const float t = __fadd_rn(__fmul_rn(cp[e0], 1.0f - a), __fmul_rn(pp[e0], a));
+                    T[pl * C::TN + r * TS + c] = t;
+                    V[pl * C::TN + r * TS + c] = fmaxf(vv, kVarMin);
+                    if constexpr (C::PACKED)
+                        if (c > 0) {
+                            smem[C::TO_OFF + pl * C::TN + r * TS + c - 1] = t;
+                            smem[C::VO_OFF + pl * C::TN + r * TS + c - 1] = fmaxf(vv, kVarMin);
+                        }
+                }
             }
         }
     }
