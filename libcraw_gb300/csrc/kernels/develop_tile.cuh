@@ -288,6 +288,29 @@ struct RcdTile {
  * the threads of a warp, one quad each, read consecutive elements of a
  * plane rather than every other one. The output planes reuse Dp's space
  * once the weights exist. */
+/* Item i of a W x H grid of quads as (x, y). With W > 32 the first 32 H
+ * items take 32 consecutive columns of one row each and the rest the
+ * W - 32 columns left over, so that the items of a warp (NT a multiple of
+ * 32) never wrap from one row to the next: a wrap lands the second row's
+ * shared-memory words on banks the first row's half-warp already uses. */
+template <int W, int H>
+CRAW_DEV void quad_item(int i, int &x, int &y)
+{
+    if constexpr (W > 32) {
+        if (i < 32 * H) {
+            x = i & 31;
+            y = i >> 5;
+            return;
+        }
+        const int e = i - 32 * H;
+        x = 32 + e % (W - 32);
+        y = e / (W - 32);
+    } else {
+        x = i % W;
+        y = i / W;
+    }
+}
+
 template <int TW, int TH, int NT>
 struct RcdQuads {
     static constexpr int QW = TW / 2, QH = TH / 2;
@@ -355,7 +378,10 @@ struct RcdQuads {
     {
         constexpr int QX = QW + 6, QY = QH + 6;
         for (int i = threadIdx.x; i < QX * QY; i += NT) {
-            int qx = i % QX - 3, qy = i / QX - 3;
+            int qx, qy;
+            quad_item<QX, QY>(i, qx, qy);
+            qx -= 3;
+            qy -= 3;
             int x = x0 + 2 * qx, y = y0 + 2 * qy;
             const char *r0 = (const char *)io.src + (size_t)y * io.src_pitch;
             uint32_t a = __ldg(reinterpret_cast<const uint32_t *>(r0) + x / 2);
@@ -372,7 +398,10 @@ struct RcdQuads {
     {
         constexpr int QX = QW + 6, QY = QH + 6;
         for (int i = threadIdx.x; i < QX * QY; i += NT) {
-            int qx = i % QX - 3, qy = i / QX - 3;
+            int qx, qy;
+            quad_item<QX, QY>(i, qx, qy);
+            qx -= 3;
+            qy -= 3;
             const uint32_t *r0 = box + (2 * qy + 6) * (BW / 2) + qx + 4;
             put_quad(k, io, qx, qy, r0[0], r0[BW / 2]);
         }
@@ -383,7 +412,10 @@ struct RcdQuads {
         /* Low pass at R and B, and the four discriminations at every
          * pixel, from the 6x6 window around the quad. */
         for (int i = threadIdx.x; i < (QW + 4) * (QH + 4); i += NT) {
-            const int qx = i % (QW + 4) - 2, qy = i / (QW + 4) - 2;
+            int qx, qy;
+            quad_item<QW + 4, QH + 4>(i, qx, qy);
+            qx -= 2;
+            qy -= 2;
             float v[6][6];
 #pragma unroll
             for (int r = 0; r < 6; r++)
@@ -421,7 +453,10 @@ struct RcdQuads {
          * pass, since it reads only its own quad's weights, green at R and
          * at B. */
         for (int i = threadIdx.x; i < (QW + 2) * (QH + 2); i += NT) {
-            const int qx = i % (QW + 2) - 1, qy = i / (QW + 2) - 1;
+            int qx, qy;
+            quad_item<QW + 2, QH + 2>(i, qx, qy);
+            qx -= 1;
+            qy -= 1;
             float wv[2][2];
             float4 h[4][2];
 #pragma unroll
@@ -459,7 +494,10 @@ struct RcdQuads {
         /* The missing colour at R (from the B diagonals) and at B (from the
          * R diagonals); each only where a later pass reads it. */
         for (int i = threadIdx.x; i < (QW + 2) * (QH + 2); i += NT) {
-            const int qx = i % (QW + 2) - 1, qy = i / (QW + 2) - 1;
+            int qx, qy;
+            quad_item<QW + 2, QH + 2>(i, qx, qy);
+            qx -= 1;
+            qy -= 1;
             const int x = 2 * qx, y = 2 * qy;
             float c_r = 0.0f, c_b = 0.0f;
             if (qx >= 0 && qy >= 0) {
