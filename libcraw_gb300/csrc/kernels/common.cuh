@@ -32,6 +32,29 @@ inline int craw_smem_attr(F fn, size_t bytes, std::atomic<uint64_t> &done)
     return 0;
 }
 
+/* Item i of a W x H grid as (x, y). With W > 32 the first 32 H items take
+ * 32 consecutive columns of one row each and the rest the W - 32 columns
+ * left over, so that the items of a warp (block sizes a multiple of 32)
+ * never wrap from one row to the next: a wrap lands the second row's
+ * shared-memory words on banks the first row's half-warp already uses. */
+template <int W, int H>
+CRAW_DEV void craw_row_item(int i, int &x, int &y)
+{
+    if constexpr (W > 32) {
+        if (i < 32 * H) {
+            x = i & 31;
+            y = i >> 5;
+            return;
+        }
+        const int e = i - 32 * H;
+        x = 32 + e % (W - 32);
+        y = e / (W - 32);
+    } else {
+        x = i % W;
+        y = i / W;
+    }
+}
+
 /* Mirror without repeating the edge sample (reference common.glsl:49-55,
  * lib/ref/ref_debayer.c:21-34), looping for tiles that hang further past
  * a small frame than one reflection reaches. n >= 2. */

@@ -288,29 +288,6 @@ struct RcdTile {
  * the threads of a warp, one quad each, read consecutive elements of a
  * plane rather than every other one. The output planes reuse Dp's space
  * once the weights exist. */
-/* Item i of a W x H grid of quads as (x, y). With W > 32 the first 32 H
- * items take 32 consecutive columns of one row each and the rest the
- * W - 32 columns left over, so that the items of a warp (NT a multiple of
- * 32) never wrap from one row to the next: a wrap lands the second row's
- * shared-memory words on banks the first row's half-warp already uses. */
-template <int W, int H>
-CRAW_DEV void quad_item(int i, int &x, int &y)
-{
-    if constexpr (W > 32) {
-        if (i < 32 * H) {
-            x = i & 31;
-            y = i >> 5;
-            return;
-        }
-        const int e = i - 32 * H;
-        x = 32 + e % (W - 32);
-        y = e / (W - 32);
-    } else {
-        x = i % W;
-        y = i / W;
-    }
-}
-
 template <int TW, int TH, int NT>
 struct RcdQuads {
     static constexpr int QW = TW / 2, QH = TH / 2;
@@ -379,7 +356,7 @@ struct RcdQuads {
         constexpr int QX = QW + 6, QY = QH + 6;
         for (int i = threadIdx.x; i < QX * QY; i += NT) {
             int qx, qy;
-            quad_item<QX, QY>(i, qx, qy);
+            craw_row_item<QX, QY>(i, qx, qy);
             qx -= 3;
             qy -= 3;
             int x = x0 + 2 * qx, y = y0 + 2 * qy;
@@ -399,7 +376,7 @@ struct RcdQuads {
         constexpr int QX = QW + 6, QY = QH + 6;
         for (int i = threadIdx.x; i < QX * QY; i += NT) {
             int qx, qy;
-            quad_item<QX, QY>(i, qx, qy);
+            craw_row_item<QX, QY>(i, qx, qy);
             qx -= 3;
             qy -= 3;
             const uint32_t *r0 = box + (2 * qy + 6) * (BW / 2) + qx + 4;
@@ -413,7 +390,7 @@ struct RcdQuads {
          * pixel, from the 6x6 window around the quad. */
         for (int i = threadIdx.x; i < (QW + 4) * (QH + 4); i += NT) {
             int qx, qy;
-            quad_item<QW + 4, QH + 4>(i, qx, qy);
+            craw_row_item<QW + 4, QH + 4>(i, qx, qy);
             qx -= 2;
             qy -= 2;
             float v[6][6];
@@ -454,7 +431,7 @@ struct RcdQuads {
          * at B. */
         for (int i = threadIdx.x; i < (QW + 2) * (QH + 2); i += NT) {
             int qx, qy;
-            quad_item<QW + 2, QH + 2>(i, qx, qy);
+            craw_row_item<QW + 2, QH + 2>(i, qx, qy);
             qx -= 1;
             qy -= 1;
             float wv[2][2];
@@ -495,7 +472,7 @@ struct RcdQuads {
          * R diagonals); each only where a later pass reads it. */
         for (int i = threadIdx.x; i < (QW + 2) * (QH + 2); i += NT) {
             int qx, qy;
-            quad_item<QW + 2, QH + 2>(i, qx, qy);
+            craw_row_item<QW + 2, QH + 2>(i, qx, qy);
             qx -= 1;
             qy -= 1;
             const int x = 2 * qx, y = 2 * qy;
