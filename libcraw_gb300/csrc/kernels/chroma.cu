@@ -47,7 +47,10 @@ k_chroma_blur(const CRAWKChroma c, const void *q, size_t q_pitch, void *qf, size
             float4 s = t[(ly + kR + dy) * SX + lx + kR + dx];
             float dg = (s.z - ctr.z) * inv_range;
             float d0 = (s.x - ctr.x) * inv_chroma, d1 = (s.y - ctr.y) * inv_chroma;
-            float w = expf(-(float)(dx * dx + dy * dy) * kInv2s2 - dg * dg - d0 * d0 - d1 * d1);
+            /* The fast exponential: its relative error (~1e-6) moves the
+             * normalised weighted mean far less than the 2e-4 the stage is
+             * held to against the oracle. */
+            float w = __expf(-(float)(dx * dx + dy * dy) * kInv2s2 - dg * dg - d0 * d0 - d1 * d1);
             a0 += w * s.x;
             a1 += w * s.y;
             ws += w;
