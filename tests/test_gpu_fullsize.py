@@ -10,7 +10,12 @@ do not need the oracle to develop the whole frame:
     crop mirrors at the same edge;
   * the frame's AWB histogram, bit for bit, against the CPU builder run on
     the whole intermediate the GPU produced;
-  * the same frame recorded twice gives the same bytes.
+  * the same frame recorded twice gives the same bytes;
+  * a three-frame temporal sequence (temporal 0.8 + NLM 1.0): in each
+    window, each frame's denoised mosaic and next state against the
+    oracle's temporal denoise of the crop, fed the crop of the state the
+    GPU left (the temporal agreement test reads one plane sample around a
+    pixel, the NLM four, well inside the margin).
 """
 import numpy as np
 import pytest
@@ -103,3 +108,53 @@ def test_awb_histogram_full_frame(developed):
 def test_recording_is_deterministic(developed):
     assert developed["same"]
     assert developed["same_keep"], "keeping the intermediate changes the output"
+
+
+@pytest.fixture(scope="module")
+def temporal_sequence():
+    """Three frames of the temporal workload at 5760x3240 (temporal 0.8 +
+    NLM 1.0): per frame the mosaic, the denoised mosaic and the state the
+    GPU left (levels and quantised variance), all at full size."""
+    c = W.workload("temporal_mhc_p3")
+    assert (c.width, c.height) == (WIDTH, HEIGHT)
+    prof = W.make_profile()
+    model = W.noise_model(c.noise_a_dn, c.noise_b_dn)
+    pp = L.pipeline_params(WIDTH, HEIGHT, debayer=L.DEBAYER_MHC, out_space=L.CS_P3D65,
+                           flags=L.FLAG_DENOISE | L.FLAG_TEMPORAL_DENOISE | L.FLAG_KEEP_INTERMEDIATE,
+                           out_format=L.FORMAT_RGBA32F)
+    fp = L.frame_params(prof, denoise_strength=1.0, denoise_temporal_strength=0.8, noise_override=model)
+    s = torch.cuda.current_stream().cuda_stream
+    frames = []
+    with L.Context(0) as ctx, L.Pipeline(ctx, pp) as pipe:
+        for f in range(3):
+            m = c.frame(f)
+            _, src = upload_mosaic(m)
+            _, dst = alloc_rgba(WIDTH, HEIGHT)
+            pipe.record(s, src, dst, fp)
+            torch.cuda.synchronize()
+            _, mos = pipe.intermediate()
+            lvl, var = pipe.temporal_state()
+            frames.append(dict(m=m, got=download_image(mos, "r16"), lvl=download_image(lvl, "r32f"),
+                               qv=(download_image(var, "r8").astype(np.float32) / 255.0) ** 2))
+    return dict(prof=prof, model=model, frames=frames)
+
+
+@pytest.mark.parametrize("win", WINDOWS, ids=[f"{x}_{y}" for x, y, _, _ in WINDOWS])
+def test_temporal_windows_vs_oracle(temporal_sequence, win):
+    """Each frame's denoised mosaic and next state in the window against the
+    oracle's temporal denoise of the crop, given the crop of the state the
+    GPU left after the previous frame (none for the first)."""
+    x, y, w, h = win
+    x0, y0 = max(0, x - MARGIN), max(0, y - MARGIN)
+    x1, y1 = min(WIDTH, x + w + MARGIN), min(HEIGHT, y + h + MARGIN)
+    sl = (slice(y - y0, y - y0 + h), slice(x - x0, x - x0 + w))
+    ts = temporal_sequence
+    prev = None
+    for f, fr in enumerate(ts["frames"]):
+        crop = np.ascontiguousarray(fr["m"][y0:y1, x0:x1])
+        clean, nxt = orc.denoise_temporal(crop, ts["prof"], ts["model"], 1.0, 0.8, prev)
+        d = np.abs(fr["got"][y:y + h, x:x + w].astype(np.int32) - clean[sl].astype(np.int32))
+        assert d.max() <= 2 and (d > 0).mean() < 0.02, (win, f, d.max(), (d > 0).mean())
+        assert np.max(np.abs(fr["lvl"][y:y + h, x:x + w] - nxt[0][sl])) < 1e-4, (win, f)
+        assert np.max(np.abs(fr["qv"][y:y + h, x:x + w] - nxt[1][sl])) < 0.01, (win, f)
+        prev = np.ascontiguousarray(np.stack([fr["lvl"][y0:y1, x0:x1], fr["qv"][y0:y1, x0:x1]]).astype(np.float32))
