@@ -15,7 +15,9 @@ do not need the oracle to develop the whole frame:
     window, each frame's denoised mosaic and next state against the
     oracle's temporal denoise of the crop, fed the crop of the state the
     GPU left (the temporal agreement test reads one plane sample around a
-    pixel, the NLM four, well inside the margin).
+    pixel, the NLM four, well inside the margin);
+  * the 16-frame batch mix at its real sizes (168 Mpx) in one batch
+    record against each frame's own single-frame pipeline.
 """
 import numpy as np
 import pytest
@@ -158,3 +160,44 @@ def test_temporal_windows_vs_oracle(temporal_sequence, win):
         assert np.max(np.abs(fr["lvl"][y:y + h, x:x + w] - nxt[0][sl])) < 1e-4, (win, f)
         assert np.max(np.abs(fr["qv"][y:y + h, x:x + w] - nxt[1][sl])) < 0.01, (win, f)
         prev = np.ascontiguousarray(np.stack([fr["lvl"][y0:y1, x0:x1], fr["qv"][y0:y1, x0:x1]]).astype(np.float32))
+
+
+def test_batch_mix_matches_single_frames():
+    """The 16-frame batch mix at its real sizes (6 x 1920x1080, 4 x
+    3840x2160, 4 x 5760x3240, 2 x 6000x4000; NLM 1.0 + RCD + BT.2020, each
+    frame its own noise model) in one craw_batch_record with the default
+    split: every frame agrees with the same frame through its own
+    single-frame pipeline within the denoised-chain bound."""
+    from gpu_util import develop
+    mix = W.batch_mix()
+    prof = W.make_profile()
+    fps = [L.frame_params(prof, denoise_strength=1.0, noise_override=W.noise_model(f.noise_a_dn, f.noise_b_dn))
+           for f in mix]
+    ms = [f.frame() for f in mix]
+    bp = L.batch_params(6000, 4000, max_frames=len(mix), debayer=L.DEBAYER_RCD, out_space=L.CS_BT2020,
+                        flags=L.FLAG_DENOISE)
+    with L.Context(0) as ctx:
+        with L.Batch(ctx, bp) as b:
+            keep, srcs, dsts, outs = [], [], [], []
+            for m in ms:
+                t, s = upload_mosaic(m)
+                o, d = alloc_rgba(m.shape[1], m.shape[0])
+                keep += [t]
+                srcs += [s]
+                dsts += [d]
+                outs += [o]
+            b.record(torch.cuda.current_stream().cuda_stream, srcs, dsts, fps)
+            torch.cuda.synchronize()
+            info = b.info()
+            got = [o.cpu().numpy() for o in outs]
+            del keep, outs
+        assert info["direct_frames"] == 10, info
+        for i, (m, fp) in enumerate(zip(ms, fps)):
+            h, w = m.shape
+            pp = L.pipeline_params(w, h, debayer=L.DEBAYER_RCD, out_space=L.CS_BT2020, flags=L.FLAG_DENOISE,
+                                   out_format=L.FORMAT_RGBA32F)
+            with L.Pipeline(ctx, pp) as pipe:
+                ref = develop(pipe, m, fp)
+            assert not np.isnan(got[i]).any(), i
+            ok, st = denoised_chain_ok(got[i], ref)
+            assert ok, (i, (w, h), st)
