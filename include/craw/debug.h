@@ -30,4 +30,31 @@ struct CRAWPipeline;
  * negative errno if the read fails. */
 CRAW_API int craw_debug_kernel_errors(struct CRAWPipeline *pipe);
 
+/* The exact rounding of the denoised codes (the samples whose float code
+ * lies near a rounding boundary re-evaluated, so that they round as a
+ * double evaluation of the filter does): `scale` sets the width of the
+ * band of samples re-evaluated, in units of the float evaluation's error
+ * bound (the default 2; 0 turns the exact rounding off; 1e6 and more
+ * re-evaluate every sample). A negative scale only reads. Returns the
+ * previous scale. For tests and measurement. */
+CRAW_API float craw_debug_denoise_round(float scale);
+
+/* on = 1 (the default): the exact rounding settles what it can of the
+ * marked samples with a float re-evaluation that bounds its own error, and
+ * evaluates the rest in double-float arithmetic; 0: every marked sample in
+ * double-float, for checking the first stage's decisions. A negative value
+ * only reads. Returns the previous setting. */
+CRAW_API int craw_debug_denoise_round_decide(int on);
+
+/* Waits for the pipeline's recordings and reads the exact rounding's
+ * statistics since the last call: counts[0] samples re-evaluated,
+ * counts[1] codes changed, counts[2] samples the float re-evaluation could
+ * not settle (evaluated in double-float); and, for up to max_records of
+ * the changed codes, four floats each: the sample's filtered value t, its
+ * code position x, the distance of the exact x from its rounding boundary
+ * (the float evaluation was off by at least that much), its plane. Clears
+ * them. Returns the records written, or a negative errno. */
+CRAW_API int craw_debug_denoise_round_stats(struct CRAWPipeline *pipe, uint32_t counts[3], float *records,
+                                            uint32_t max_records);
+
 #endif /* CRAW_DEBUG_H */

@@ -281,7 +281,8 @@ for _s, _n in ((Profile, 1264), (FrameParams, 264), (PipelineParams, 256), (Cuda
 EXPORTS = (
     "craw_version_int", "craw_log", "craw_context_create", "craw_context_free",
     "craw_cuda_check_device", "craw_debug_fail_alloc", "craw_debug_force_denoise_shape",
-    "craw_debug_rcd_tma", "craw_debug_kernel_errors",
+    "craw_debug_rcd_tma", "craw_debug_kernel_errors", "craw_debug_denoise_round",
+    "craw_debug_denoise_round_decide", "craw_debug_denoise_round_stats",
     "craw_pipeline_params_init", "craw_frame_params_init", "craw_pipeline_create",
     "craw_pipeline_free", "craw_pipeline_record", "craw_pipeline_get_awb_histogram",
     "craw_pipeline_get_awb_histogram_n", "craw_pipeline_get_stage_times",
@@ -363,6 +364,9 @@ def lib() -> C.CDLL:
         "craw_debug_force_denoise_shape": (i32, [i32]),
         "craw_debug_rcd_tma": (i32, [i32]),
         "craw_debug_kernel_errors": (i32, [vp]),
+        "craw_debug_denoise_round": (C.c_float, [C.c_float]),
+        "craw_debug_denoise_round_decide": (i32, [i32]),
+        "craw_debug_denoise_round_stats": (i32, [vp, C.POINTER(C.c_uint32), vp, C.c_uint32]),
         "craw_pipeline_params_init": (None, [C.POINTER(PipelineParams)]),
         "craw_frame_params_init": (None, [C.POINTER(FrameParams)]),
         "craw_pipeline_create": (i32, [vp, C.POINTER(PipelineParams), C.POINTER(vp)]),
@@ -646,6 +650,19 @@ class Pipeline:
         pipeline's kernels set: 0 when all is well."""
         return _check(lib().craw_debug_kernel_errors(self._h), "craw_debug_kernel_errors")
 
+    def round_stats(self, max_records: int = 4096):
+        """Waits for the device and returns (and clears) the exact rounding's
+        statistics: (samples re-evaluated, codes changed, records, samples
+        evaluated in double-float), records an (n, 4) float32 array of (t,
+        x, distance of the exact x from its rounding boundary, plane) per
+        changed code."""
+        import numpy as np
+        counts = (C.c_uint32 * 3)()
+        rec = np.zeros((max_records, 4), np.float32)
+        n = _check(lib().craw_debug_denoise_round_stats(self._h, counts, rec.ctypes.data, max_records),
+                   "craw_debug_denoise_round_stats")
+        return int(counts[0]), int(counts[1]), rec[:n], int(counts[2])
+
     def temporal_state(self) -> tuple[Image, Image]:
         lvl, var = Image(), Image()
         _check(lib().craw_pipeline_get_temporal_state(self._h, C.byref(lvl), C.byref(var)),
@@ -858,6 +875,19 @@ def debug_force_denoise_shape(shape: int) -> None:
     """Every pipeline created from now uses denoise shape `shape` (-1: the
     autotuner's)."""
     _check(lib().craw_debug_force_denoise_shape(shape), "craw_debug_force_denoise_shape")
+
+
+def debug_denoise_round(scale: float) -> float:
+    """Width of the exact rounding's band in units of the float error bound
+    (default 2; 0: off; 1e6: every sample); a negative scale only reads.
+    Returns the previous scale."""
+    return float(lib().craw_debug_denoise_round(scale))
+
+
+def debug_denoise_round_decide(on: int) -> int:
+    """1 (default): the float decision stage settles what it can of the
+    marked samples; 0: all of them in double-float; -1 only reads."""
+    return int(lib().craw_debug_denoise_round_decide(on))
 
 
 def debug_rcd_tma(on: bool) -> bool:

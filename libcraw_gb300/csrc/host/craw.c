@@ -165,6 +165,27 @@ CRAW_API int craw_debug_force_denoise_shape(int shape)
     return 0;
 }
 
+/* The marking band of the exact denoise rounding, in units of the float
+ * path's error bound, and whether its float decision stage runs. */
+float craw_round_scale = 2.0f;
+int craw_round_decide = 1;
+
+CRAW_API float craw_debug_denoise_round(float scale)
+{
+    const float was = craw_round_scale;
+    if (scale >= 0.0f)
+        craw_round_scale = scale;
+    return was;
+}
+
+CRAW_API int craw_debug_denoise_round_decide(int on)
+{
+    const int was = craw_round_decide;
+    if (on >= 0)
+        craw_round_decide = on ? 1 : 0;
+    return was;
+}
+
 CRAW_API void craw_debug_fail_alloc(int k)
 {
     craw_fail_countdown = k;

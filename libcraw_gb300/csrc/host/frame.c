@@ -111,7 +111,7 @@ int craw_develop_consts(CRAWContext *ctx, uint32_t w, uint32_t h, int debayer, b
 }
 
 int craw_denoise_consts(CRAWContext *ctx, uint32_t w, uint32_t h, const CRAWFrameParams *fp, int mode,
-                        CRAWKDenoise *k)
+                        CRAWKDenoise *k, CRAWKDenoiseExact *ex)
 {
     CRAWNoiseModel nm;
     float a, b, c, hs;
@@ -159,5 +159,86 @@ int craw_denoise_consts(CRAWContext *ctx, uint32_t w, uint32_t h, const CRAWFram
         k->inv_range[s] = 1.0f / range;
         k->range[s] = range;
     }
+    if (ex)
+        craw_denoise_exact_consts(k, fp->profile, nm.a, b, hs, ex);
     return 0;
+}
+
+/* A double split into two floats: hi the nearest float, lo the nearest
+ * float to the rest (together within 2^-48 relative of v). */
+static void split(double v, float out[2])
+{
+    out[0] = (float)v;
+    out[1] = (float)(v - (double)out[0]);
+}
+
+void craw_denoise_exact_consts(const CRAWKDenoise *k, const CRAWProfile *prof, float a, float b, float strength,
+                               CRAWKDenoiseExact *ex)
+{
+    /* The reference's arithmetic in double (lib/ref/ref_denoise.c:25-58,
+     * 173-336 with R = double): the noise model, the levels and the
+     * strength are floats and enter exactly. */
+    const double ad = a, cd = 3.0 * ad * ad / 8.0 + (double)b, h = strength > 0.0f ? strength : 1.0;
+    const double sc = sqrt(cd), fwd = 2.0 / ad;
+    double bmax = 0.0;
+    memset(ex, 0, sizeof(*ex));
+    ex->pw = k->pw;
+    ex->ph = k->ph;
+    ex->mode = k->mode;
+    for (int s = 0; s < 4; s++) {
+        const double blk = (double)prof->black_level[s], rng = (double)prof->white_level[s] - blk;
+        split(blk, ex->black[s]);
+        split(rng, ex->range[s]);
+        split(1.0 / rng, ex->inv_range[s]);
+        /* The float decision stage. */
+        ex->k1[s] = (float)(1.0 / (65535.0 * rng));
+        ex->k0[s] = (float)(blk / rng);
+        ex->q[s] = (float)(4.0 / (65535.0 * rng * ad));
+        ex->k2[s] = (float)(65535.0 * rng * ad / 4.0);
+        split(4.0 / (65535.0 * rng * ad), ex->qq[s]);
+        split(4.0 * cd / (ad * ad) - 4.0 * blk / (ad * rng), ex->beta[s]);
+        bmax = fmax(bmax, blk);
+    }
+    split(1.0 / 65535.0, ex->inv65535);
+    ex->gat_a = a;
+    split(cd, ex->gat_c);
+    split(sc, ex->gat_sc);
+    split(1.0 / sc, ex->gat_isc);
+    split(fwd, ex->gat_fwd);
+    split(ad / 4.0, ex->gat_inv);
+    split(cd / ad, ex->gat_off);
+    split(fwd * sc, ex->gat_t0);
+    split((1.0 / 9.0) * (1.0 / (h * h)), ex->k_nlm);
+    split((double)DN_GUARD_LO, ex->guard_lo);
+    split(1.0 / ((double)DN_GUARD_HI - (double)DN_GUARD_LO), ex->guard_inv);
+    ex->kn = (float)((1.0 / 9.0) / (h * h));
+    ex->c1 = (float)(-1.4426950408889634 * (1.0 / 9.0) / (h * h));
+    ex->c0 = (float)(2.0 * 1.4426950408889634);
+    ex->dark_code = (uint32_t)ceil(bmax * 65535.0) + 1u;
+    ex->decide = craw_round_decide;
+}
+
+void craw_denoise_round_band(const CRAWKDenoise *k, float scale, CRAWKRound *rd)
+{
+    /* The float path's error in codes, about B ulps of t carried through
+     * dx/dt = 65535 range (a/2) t (the inverse transform), plus a few ulps
+     * of x itself (x <= 65535 black + 65535 range a/4 t^2) and of t near
+     * the transform's linear branch. With B = 16 the band at scale 1 is
+     * about twice the largest error seen in the float evaluation; `scale`
+     * multiplies the whole band. */
+    const double B = 16.0 * 0x1p-24, X = 4.0 * 0x1p-24;
+    double rmax = 0.0, bmax = 0.0;
+    for (int s = 0; s < 4; s++) {
+        rmax = fmax(rmax, (double)k->range[s]);
+        bmax = fmax(bmax, (double)k->black[s]);
+    }
+    const double a = k->gat_a;
+    rd->c2 = (float)(scale * (B * 65535.0 * rmax * a / 2.0 + X * 65535.0 * rmax * a / 4.0));
+    rd->c0 = (float)(scale * (B * 65535.0 * rmax * ((double)k->gat_sc + a / 2.0 * (double)k->gat_t0) *
+                              ((double)k->gat_t0 + 1.0) + X * 65535.0 * bmax));
+    if (scale >= 1e6f) {
+        /* Every sample. */
+        rd->c0 = 1.0f;
+        rd->c2 = 0.0f;
+    }
 }

@@ -47,7 +47,21 @@ bool craw_images_overlap(const CRAWImage *a, const CRAWImage *b);
 int craw_develop_consts(CRAWContext *ctx, uint32_t w, uint32_t h, int debayer, bool fp16,
                         enum CRAWColorSpace default_space, const CRAWFrameParams *fp, CRAWKDevelop *dk);
 int craw_denoise_consts(CRAWContext *ctx, uint32_t w, uint32_t h, const CRAWFrameParams *fp, int mode,
-                        CRAWKDenoise *k);
+                        CRAWKDenoise *k, CRAWKDenoiseExact *ex);
+/* The constants of the exact rounding (ex), from the float constants k of
+ * the same frame, its profile, noise model and strength. */
+void craw_denoise_exact_consts(const CRAWKDenoise *k, const CRAWProfile *prof, float a, float b, float strength,
+                               CRAWKDenoiseExact *ex);
+/* The marking band of the exact rounding for the frame k describes,
+ * `scale` times the float path's error bound (1e6 and above: every
+ * sample); rd->flags and rd->count2 are left alone. */
+void craw_denoise_round_band(const CRAWKDenoise *k, float scale, CRAWKRound *rd);
+
+/* craw_debug_denoise_round(): the scale of the marking band (0: the exact
+ * rounding is off); craw_debug_denoise_round_decide(): 0 sends every
+ * marked sample to the double-float stage. */
+extern float craw_round_scale;
+extern int craw_round_decide;
 
 /* Bins one deferred AWB block on the host, with the CPU builder's
  * arithmetic (lib/awb.c:270-291 of the reference). */

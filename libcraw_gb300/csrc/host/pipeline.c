@@ -28,6 +28,7 @@
 
 #include <cuda_runtime_api.h>
 
+#include <craw/debug.h>
 #include <craw/pipeline.h>
 
 #include "internal.h"
@@ -43,12 +44,14 @@ static_assert(sizeof(CRAWCudaInitParams) == 64, "CRAWCudaInitParams size");
 
 #define MAX_STAGES 16
 
-enum { ST_DENOISE, ST_DEVELOP, ST_BLUR, ST_UP, ST_AWB, ST_HL, ST_NB };
+enum { ST_DENOISE, ST_DEVELOP, ST_BLUR, ST_UP, ST_AWB, ST_HL, ST_ROUND, ST_NB };
 static const char *const stage_names[ST_NB] = {
     "denoise_nlm", "develop", "chroma_blur", "chroma_up_color", "awb_reduce", "highlights",
+    "denoise_round",
 };
 static const char *const plain_stage_names[ST_NB] = {
     "plain_denoise", "plain_develop", "plain_chroma", "plain_chroma", "plain_awb", "highlights",
+    "denoise_round",
 };
 
 /* One host-visible AWB slot: the three histograms, then the deferred
@@ -87,6 +90,9 @@ struct CRAWPipeline {
     uint8_t *awb_dev;         /* HIST_BYTES + DEFER_BYTES + 4, mirrors a slot */
     uint32_t nb_blocks;
     uint32_t *kerr;           /* CRAW_K_ERR_* bits the kernels set */
+    uint32_t *round_flags;    /* marks of the exact rounding, CRAW_K_ROUND_WORDS */
+    uint32_t *round_stats;    /* its statistics, CRAW_K_ROUND_STATS_BYTES */
+    uint32_t *round_list;     /* undecided samples, CRAW_K_ROUND_LIST entries, then their count */
 
     /* Plain-pipeline scratch. */
     float *p_v, *p_scratch, *p_t, *p_var;
@@ -137,7 +143,7 @@ static void release(CRAWPipeline *p)
     void *bufs[] = {
         p->clean, p->lvl[0], p->lvl[1], p->var[0], p->var[1], p->inter, p->q, p->qf,
         p->awb_rec, p->awb_dev, p->kerr, p->p_v, p->p_scratch, p->p_t, p->p_var,
-        p->hl_mosaic, p->hl_levels,
+        p->hl_mosaic, p->hl_levels, p->round_flags, p->round_stats, p->round_list,
     };
     cudaSetDevice(ctx->device);
     for (size_t i = 0; i < CRAW_ARRAY_ELEMS(bufs); i++)
@@ -201,7 +207,7 @@ static int time_denoise(CRAWPipeline *p, const CRAWKDenoise *k, const CRAWKDenoi
     for (int r = 0; r < 4 && ret == 0; r++) {
         float t = 0.0f;
         cudaEventRecord(e0, ctx->stream);
-        ret = craw_k_denoise(k, io, shape, ctx->stream);
+        ret = craw_k_denoise(k, io, shape, NULL, ctx->stream);
         cudaEventRecord(e1, ctx->stream);
         if (ret == 0 && cudaEventSynchronize(e1) == cudaSuccess &&
             cudaEventElapsedTime(&t, e0, e1) == cudaSuccess && r > 0 && t < *ms)
@@ -323,6 +329,29 @@ CRAW_API int craw_debug_kernel_errors(CRAWPipeline *p)
         cudaMemset(p->kerr, 0, sizeof(bits)) != cudaSuccess)
         return CRAW_ERROR(EIO);
     return (int)bits;
+}
+
+CRAW_API int craw_debug_denoise_round_stats(CRAWPipeline *p, uint32_t counts[3], float *records,
+                                            uint32_t max_records)
+{
+    uint32_t head[4];
+    if (!p || !counts || (max_records && !records))
+        return CRAW_ERROR(EINVAL);
+    if (!p->round_stats)
+        return CRAW_ERROR(ENOTSUP);
+    cudaSetDevice(p->ctx->device);
+    if (cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemcpy(head, p->round_stats, sizeof(head), cudaMemcpyDeviceToHost) != cudaSuccess)
+        return CRAW_ERROR(EIO);
+    counts[0] = head[0];
+    counts[1] = head[1];
+    counts[2] = head[3];
+    uint32_t nr = CRAW_MIN(CRAW_MIN(head[2], (uint32_t)CRAW_K_ROUND_RECORDS), max_records);
+    if (nr && cudaMemcpy(records, p->round_stats + 4, (size_t)nr * 16, cudaMemcpyDeviceToHost) != cudaSuccess)
+        return CRAW_ERROR(EIO);
+    if (cudaMemset(p->round_stats, 0, CRAW_K_ROUND_STATS_BYTES) != cudaSuccess)
+        return CRAW_ERROR(EIO);
+    return (int)nr;
 }
 
 CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *params,
@@ -466,6 +495,22 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
     }
     if ((ret = craw_dev_alloc(ctx, (void **)&p->kerr, 16)) < 0)
         goto fail;
+    if (p->has_denoise && !p->plain) {
+        /* The exact rounding: its marks (a bit per sample, 2.3 MB at
+         * 5760x3240), the list of samples its float stage cannot settle
+         * (a sixteenth of the samples and their count: 4.9 MB) and its
+         * statistics. */
+        if ((ret = craw_dev_alloc(ctx, (void **)&p->round_flags,
+                                  CRAW_K_ROUND_WORDS(w / 2, h / 2) * sizeof(uint32_t))) < 0 ||
+            (ret = craw_dev_alloc(ctx, (void **)&p->round_stats, CRAW_K_ROUND_STATS_BYTES)) < 0 ||
+            (ret = craw_dev_alloc(ctx, (void **)&p->round_list,
+                                  (CRAW_K_ROUND_LIST(w / 2, h / 2) + 4) * sizeof(uint32_t))) < 0)
+            goto fail;
+        if (cudaMemsetAsync(p->round_stats, 0, CRAW_K_ROUND_STATS_BYTES, ctx->stream) != cudaSuccess) {
+            ret = CRAW_ERROR(EIO);
+            goto fail;
+        }
+    }
     if (cudaMemsetAsync(p->kerr, 0, 16, ctx->stream) != cudaSuccess) {
         ret = CRAW_ERROR(EIO);
         goto fail;
@@ -548,6 +593,9 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
     CRAWKDevelop dk;
     CRAWKDevelopIO dio;
     CRAWKDenoise dnk;
+    CRAWKDenoiseExact dnx;
+    CRAWKRound rd = { 0 };
+    bool exact = false;
     CRAWKChroma ck;
     struct prof_ctx pc = { 0 };
     bool spatial, temporal, replay, denoise, chroma;
@@ -593,8 +641,16 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
     if (denoise) {
         dn_mode = (spatial ? CRAW_K_DN_SPATIAL : 0) | (temporal ? CRAW_K_DN_TEMPORAL : 0) |
                   (temporal && t_read >= 0 ? CRAW_K_DN_HISTORY : 0);
-        if ((ret = craw_denoise_consts(ctx, w, h, fp, dn_mode, &dnk)) < 0)
+        /* The exact rounding of the codes: the spatial filter without a
+         * temporal history (the other modes round as the float path does). */
+        exact = !p->plain && p->round_flags && dn_mode == CRAW_K_DN_SPATIAL && craw_round_scale > 0.0f;
+        if ((ret = craw_denoise_consts(ctx, w, h, fp, dn_mode, &dnk, exact ? &dnx : NULL)) < 0)
             return ret;
+        if (exact) {
+            craw_denoise_round_band(&dnk, craw_round_scale, &rd);
+            rd.flags = p->round_flags;
+            rd.count2 = p->round_list + CRAW_K_ROUND_LIST(w / 2, h / 2);
+        }
     }
 
     chroma = p->has_chroma && fp->denoise_chroma_strength > 0.0f;
@@ -642,10 +698,18 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
         }
         prof_begin(&pc, ST_DENOISE);
         ret = p->plain ? craw_k_plain_denoise(&dnk, &io, p->p_t, p->p_var, s)
-                       : craw_k_denoise(&dnk, &io, p->dn_shape[(dn_mode & CRAW_K_DN_HISTORY) != 0], s);
+                       : craw_k_denoise(&dnk, &io, p->dn_shape[(dn_mode & CRAW_K_DN_HISTORY) != 0],
+                                        exact ? &rd : NULL, s);
         prof_end(&pc);
         if (ret < 0)
             goto launch_fail;
+        if (exact) {
+            prof_begin(&pc, ST_ROUND);
+            ret = craw_k_denoise_round(&dnk, &dnx, &io, &rd, p->round_list, p->round_stats, ctx->sm_count, s);
+            prof_end(&pc);
+            if (ret < 0)
+                goto launch_fail;
+        }
         mosaic = p->clean;
         mosaic_pitch = p->clean_pitch;
     }

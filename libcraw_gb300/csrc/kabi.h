@@ -51,8 +51,82 @@ enum CRAWKDenoiseShape {
     CRAW_K_DN_SHAPE_NB,
 };
 
+/* Exact rounding of the denoised mosaic. The denoise re-encodes its result
+ * to 16-bit codes (reference lib/ref/ref_denoise.c:318-323), so a float
+ * evaluation and a double one disagree by a code wherever the value lies
+ * within the float error of a rounding boundary. The denoise kernel marks
+ * every sample whose float code position x lies within
+ * band = c0 + c2 t^2 of a boundary (t: the sample's filtered value in the
+ * stabilised domain; the float error grows as t^2 because the codes per
+ * unit of t and the rounding of t both grow with t), one bit per sample;
+ * craw_k_denoise_round settles the marked samples and rewrites their codes
+ * as the double evaluation rounds them. */
+typedef struct CRAWKRound {
+    uint32_t *flags;    /* CRAW_K_ROUND_WORDS(pw, ph) words; NULL: no marking */
+    uint32_t *count2;   /* the length of the list of undecided samples: the
+                         * denoise kernel zeroes it */
+    float c0, c2;
+} CRAWKRound;
+
+/* Marks of plane p, plane row y, columns 32 w .. 32 w + 31: word
+ * (p * ph + y) * CRAW_K_ROUND_WW(pw) + w, bit b < 16 for column
+ * 32 w + 2 b, bit 16 + b for column 32 w + 2 b + 1 (the layout of a
+ * half-warp's two columns a lane). */
+#define CRAW_K_ROUND_WW(pw) (((pw) + 31) / 32)
+#define CRAW_K_ROUND_WORDS(pw, ph) ((size_t)4 * (size_t)(ph) * (size_t)CRAW_K_ROUND_WW(pw))
+
+/* The constants of the re-evaluation. Each {hi, lo} is a double value of
+ * the reference's double-precision arithmetic split into two floats
+ * (lib/ref/ref_denoise.c:25-58, 109-154, 298-324 evaluated in double);
+ * the plain floats serve the float decision stage. */
+typedef struct CRAWKDenoiseExact {
+    int32_t pw, ph, mode;                   /* mode: CRAW_K_DN_* of the frame */
+    float black[4][2], range[4][2], inv_range[4][2];
+    float inv65535[2];
+    float gat_a;                            /* the model's a (a float: exact) */
+    float gat_c[2], gat_isc[2], gat_sc[2], gat_fwd[2], gat_inv[2], gat_off[2], gat_t0[2];
+    float k_nlm[2];                         /* (1/9) / strength^2 */
+    float guard_lo[2], guard_inv[2];
+    /* Decision stage, per quad site: u = raw k1 - k0; the stabilised value
+     * of a code is t = sqrt(q raw + beta) (q = 4 / (65535 range a),
+     * beta = 4 c / a^2 - 4 black / (a range)), so q also turns a code
+     * difference into t^2 - t'^2; k2 = 65535 range a / 4 turns
+     * m^2 - m'^2 back into codes. */
+    float k1[4], k0[4], q[4], k2[4];
+    float qq[4][2], beta[4][2];             /* q and beta as double-floats */
+    float kn, c1, c0;                       /* 1/(9 h^2); -log2(e) kn, 2 log2(e) */
+    uint32_t dark_code;                     /* codes at or below it (black and the code
+                                             * above) go to the double-float stage */
+    int32_t decide;                         /* 0: every marked sample to the exact stage */
+} CRAWKDenoiseExact;
+
+/* The statistics craw_k_denoise_round keeps (device words, never reset by
+ * the kernels): [0] samples the decision stage examined, [1] codes
+ * changed, [2] records written, [3] samples listed for the double-float
+ * stage; then for each changed code, up to CRAW_K_ROUND_RECORDS, four
+ * floats: the sample's t and x, the distance of the exact x from its
+ * rounding boundary (the float evaluation was off by at least that much),
+ * the plane. */
+#define CRAW_K_ROUND_RECORDS 4096
+#define CRAW_K_ROUND_STATS_BYTES (16 + 16 * CRAW_K_ROUND_RECORDS)
+
+/* Entries of the undecided-sample list, for a frame of plane size pw x ph. */
+#define CRAW_K_ROUND_LIST(pw, ph) (((size_t)4 * (pw) * (ph)) / 16 + 65536)
+
+/* rd: NULL, or the marking of samples near a code boundary. */
 int craw_k_denoise(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, int shape,
-                   cudaStream_t s);
+                   const CRAWKRound *rd, cudaStream_t s);
+
+/* Settles the samples `rd->flags` marks (of the frame k/io describe, whose
+ * denoised mosaic io->dst the denoise kernel wrote) and rewrites their
+ * codes in io->dst as a double evaluation rounds them: a float decision
+ * stage with a bound on its own error settles most of them; the rest
+ * (rd->count2 entries of `list`, at most CRAW_K_ROUND_LIST) are evaluated
+ * in double-float arithmetic. Spatial filtering without a temporal
+ * history only (e->mode). */
+int craw_k_denoise_round(const CRAWKDenoise *k, const CRAWKDenoiseExact *e, const CRAWKDenoiseIO *io,
+                         const CRAWKRound *rd, uint32_t *list, uint32_t *stats, int sm_count,
+                         cudaStream_t s);
 
 /* The plain baseline: one kernel for the transform and the temporal
  * average into full FP32 planes (`t` and `var`, 4 planes of pw x ph each),

@@ -1,0 +1,435 @@
+/*
+ * Exact rounding of the denoised mosaic.
+ *
+ * The denoise ends by re-encoding each filtered sample as a 16-bit code,
+ * rint(clamp(black + u * range) * 65535) (reference
+ * lib/ref/ref_denoise.c:318-323). The float evaluation of the filter is
+ * within about 1e-6 relative of the exact value, so wherever the exact
+ * code position x lies within that error of a half-integer, float and
+ * double evaluations round to neighbouring codes; one code is up to 1e-2
+ * of a dark pixel, far beyond a 1e-3 bound on the developed output.
+ *
+ * The denoise kernel marks the samples whose float x lies within a band
+ * around a boundary (CRAWKRound). Two kernels here settle them:
+ *
+ * k_round_decide  takes the marked samples off the bit map (a warp's
+ *   lanes share out the set bits of 32 KW words at a time) and evaluates
+ *   each again in float, GA lanes a sample, in a form whose error it can
+ *   bound: every stabilised value of the 9x9 window as its difference from
+ *   the value m_c of the code the float path chose, computed without
+ *   cancellation from the exact integer difference of the codes,
+ *     t_k - m_c = (t_k^2 - m_c^2) / (t_k + m_c),
+ *     t_k^2 - m_c^2 = 4 (r_k - code) / (65535 range a),
+ *   the weights from these differences, and the code offset
+ *     y = x - code = (65535 range a / 4) m' (2 m_c + m'),  m' = m - m_c,
+ *   with a bound on the error of y from the unit roundoff of each step.
+ *   When y +- bound rounds the same way, that is the code a double
+ *   evaluation gives; otherwise (and for every sample near the white
+ *   guard, at or below black, or at the ends of the code range) the sample
+ *   goes to a list;
+ * k_round_exact  evaluates each listed sample in double-float arithmetic
+ *   (dfloat.cuh, about 1e-13 relative; the double evaluation's own error
+ *   is about 1e-15), G lanes a sample: the window stabilised
+ *   (ref_denoise.c:30-58), the 49 patch distances and weights
+ *   exp(-max(d2/(9 h^2) - 2, 0)) (ref_denoise.c:109-154), the weighted
+ *   mean, the inverse transform, the highlight guard and the re-encoding
+ *   (ref_denoise.c:298-324).
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "common.cuh"
+#include "dfloat.cuh"
+
+namespace {
+
+constexpr int NT = 128;                /* threads per CTA */
+constexpr int WIN = 9;                 /* search 3 + patch 1, both sides */
+constexpr int KW = 4;                  /* bit-map words a lane scans a step */
+constexpr int GA = 4;                  /* lanes of the decision stage a sample */
+constexpr int G = 8;                   /* lanes of the exact stage a sample */
+constexpr float U = 0x1p-24f;          /* float unit roundoff */
+
+/* ------------------------------------------------------------ helpers */
+
+CRAW_DEV const uint16_t *row16(const void *base, size_t pitch, int y)
+{
+    return (const uint16_t *)((const char *)base + (size_t)y * pitch);
+}
+
+CRAW_DEV void record_change(uint32_t *stats, float t, float x, float dist, int pl)
+{
+    atomicAdd(&stats[1], 1u);
+    const uint32_t r = atomicAdd(&stats[2], 1u);
+    if (r < CRAW_K_ROUND_RECORDS) {
+        float4 rec;
+        rec.x = t;
+        rec.y = x;
+        rec.z = dist;
+        rec.w = (float)pl;
+        reinterpret_cast<float4 *>(stats + 4)[r] = rec;
+    }
+}
+
+/* ------------------------------------------- the float decision stage */
+
+/* The stabilised value of a code above black, sqrt(q raw + beta), the
+ * root's argument formed in double-float (it cancels near black) and
+ * rounded once: within 1 ulp. */
+CRAW_DEV float stab(const CRAWKDenoiseExact &e, int pl, uint32_t raw)
+{
+    const float r = (float)raw;
+    const float p = e.qq[pl][0] * r;
+    float lo = fmaf(e.qq[pl][0], r, -p);
+    lo = fmaf(e.qq[pl][1], r, lo);
+    const dfl sm = df_two_sum(p, e.beta[pl][0]);
+    return sqrtf(sm.hi + (sm.lo + (lo + e.beta[pl][1])));
+}
+
+/* Settles sample (pl, qx, qy) with the GA lanes of a group (g = 0 .. GA-1,
+ * D the group's 81 floats of shared memory): true on every lane of the
+ * group when the code in io.dst is now the double evaluation's. Every
+ * lane of the warp calls it (valid false where there is no sample), so
+ * that the warp's synchronisations match.
+ *
+ * Error bound (u = 2^-24): each window value is the stabilised value t_k
+ * less m_c, d_k = (r_k - code) q / (t_k + m_c), within 5u of itself (q
+ * and the product 1u; t_k and m_c within 1u, so the denominator 1.5u; the
+ * correctly rounded reciprocal and its product 1u). A patch distance's
+ * error is then at most 10u sum |e| (|a| + |b|) + 12u d2 (e = a - b per
+ * tap: its own rounding, the square's and the sum's), and
+ * sum |e| (|a| + |b|) <= sqrt(2 d2 (P_c + P_i)) (Cauchy-Schwarz; P: a
+ * patch's sum of d^2); a weight's relative error is 1/(9h^2) times that,
+ * plus its argument's rounding (0.7u |log2 w|) and the exponential's (8u).
+ * The weighted sum's rounding is bounded as it runs (u times the sum of
+ * the partial sums' magnitudes); the weight sum's is at most 16u of it. */
+CRAW_DEV bool decide(const CRAWKDenoise &k, const CRAWKDenoiseExact &e, const CRAWKDenoiseIO &io, int pl,
+                     int qx, int qy, bool valid, int g, int lane, float *D, uint32_t *stats)
+{
+    const int px = pl & 1, py = pl >> 1;
+    const int my = 2 * qy + py, mx = 2 * qx + px;
+    bool ok = valid && e.decide;
+    int code = 0;
+    if (ok) {
+        const uint32_t raw0 = row16(io.src, io.src_pitch, my)[mx];
+        if (fmaf((float)raw0, e.k1[pl], -e.k0[pl]) >= k.guard_lo - 1e-3f)
+            ok = false;                     /* the white guard blends: exact stage */
+        code = row16(io.dst, io.dst_pitch, my)[mx];
+        if (code <= (int)e.dark_code + 2 || code >= 65534)
+            ok = false;                     /* near black (the linear branch) or the clamp */
+    }
+    const float mc = stab(e, pl, (uint32_t)code);
+    const float q = e.q[pl];
+    if (ok) {
+        const bool inner = qy >= 4 && qy + 4 < k.ph && qx >= 4 && qx + 4 < k.pw;
+        for (int s = g; s < WIN * WIN; s += GA) {
+            int yy = qy + s / WIN - 4, xx = qx + s % WIN - 4;
+            if (!inner) {
+                yy = craw_mirror(yy, k.ph);
+                xx = craw_mirror(xx, k.pw);
+            }
+            const uint32_t r = row16(io.src, io.src_pitch, 2 * yy + py)[2 * xx + px];
+            if (r <= e.dark_code)
+                ok = false;                 /* a sample at or below black: exact stage */
+            D[s] = (float)((int)r - code) * q * __frcp_rn(stab(e, pl, r) + mc);
+        }
+    }
+    /* The group goes on only if all its lanes may. */
+    const uint32_t gmask = ((1u << GA) - 1u) << (lane & ~(GA - 1));
+    ok = (__ballot_sync(0xffffffffu, ok) & gmask) == gmask;
+    __syncwarp();
+
+    float s = 0.0f, es = 0.0f, wt = 0.0f, a = 0.0f, b = 0.0f, r = 0.0f;
+    if (ok) {
+        float pc = 0.0f;
+#pragma unroll
+        for (int ky = -1; ky <= 1; ky++)
+#pragma unroll
+            for (int kx = -1; kx <= 1; kx++) {
+                const float d = D[(4 + ky) * WIN + 4 + kx];
+                pc = fmaf(d, d, pc);
+            }
+        for (int o = g; o < 49; o += GA) {
+            const int dy = o / 7 - 3, dx = o % 7 - 3;
+            float d2 = 0.0f, pi = 0.0f;
+#pragma unroll
+            for (int ky = -1; ky <= 1; ky++)
+#pragma unroll
+                for (int kx = -1; kx <= 1; kx++) {
+                    const float bb = D[(4 + dy + ky) * WIN + 4 + dx + kx];
+                    const float df = D[(4 + ky) * WIN + 4 + kx] - bb;
+                    d2 = fmaf(df, df, d2);
+                    pi = fmaf(bb, bb, pi);
+                }
+            const float xa = fmaf(d2, e.c1, e.c0);
+            const float w = craw_ex2(fminf(xa, 0.0f));
+            const float cs = sqrtf(2.0f * d2 * (pc + pi));
+            const float rho = U * fmaf(e.kn, fmaf(10.0f, cs, 12.0f * d2), fmaf(0.7f, fabsf(xa), 8.0f));
+            const float dc = D[(4 + dy) * WIN + 4 + dx];
+            const float wr = w * rho;
+            s = fmaf(w, dc, s);
+            es += fabsf(s);
+            wt += w;
+            a = fmaf(w, fabsf(dc), a);
+            b = fmaf(wr, fabsf(dc), b);
+            r += wr;
+        }
+    }
+#pragma unroll
+    for (int m = 1; m < GA; m <<= 1) {
+        s += __shfl_xor_sync(0xffffffffu, s, m);
+        es += __shfl_xor_sync(0xffffffffu, es, m) + fabsf(s);
+        wt += __shfl_xor_sync(0xffffffffu, wt, m);
+        a += __shfl_xor_sync(0xffffffffu, a, m);
+        b += __shfl_xor_sync(0xffffffffu, b, m);
+        r += __shfl_xor_sync(0xffffffffu, r, m);
+    }
+    __syncwarp();
+    if (!ok)
+        return false;
+    const float mp = s / wt;
+    const float em = (5.0f * U * a + U * es + b) / wt + fabsf(mp) * (16.0f * U + r / wt);
+    const float k2 = e.k2[pl];
+    const float y = k2 * mp * (2.0f * mc + mp);
+    const float ey = k2 * (2.0f * mc + 2.0f * fabsf(mp)) * em + 10.0f * U * fabsf(y);
+    const float n = rintf(y);
+    const float dist = 0.5f - fabsf(y - n);
+    if (!(dist > ey * 1.25f + 1e-7f))
+        return false;
+    if (n != 0.0f && g == 0) {
+        const int nc = code + (int)n;
+        ((uint16_t *)((char *)io.dst + (size_t)my * io.dst_pitch))[mx] = (uint16_t)nc;
+        record_change(stats, mc + mp, (float)nc + (y - n), dist, pl);
+    }
+    return true;
+}
+
+/* Hands out the marked samples of 32 * KW bit-map words (from `first`) to
+ * the groups of GA lanes of a warp, 32 / GA at a time: fn(pl, qx, qy,
+ * valid) runs on every lane (valid false in groups without a sample) so
+ * that the warp stays converged. */
+template <typename F>
+CRAW_DEV void walk_marks(const uint32_t *flags, long long nwords, int ww, int ph, long long first, int lane,
+                         F &&fn)
+{
+    int cnt = 0;
+#pragma unroll
+    for (int j = 0; j < KW; j++) {
+        const long long i = first + (long long)lane * KW + j;
+        cnt += __popc(i < nwords ? __ldg(flags + i) : 0u);
+    }
+    int incl = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o)
+            incl += v;
+    }
+    const int tot = __shfl_sync(0xffffffffu, incl, 31);
+    const int excl = incl - cnt;
+    for (int b = 0; b < tot; b += 32 / GA) {
+        const int idx = b + lane / GA;
+        /* The lane holding entry idx: the first with incl > idx. */
+        int lo = 0, hi = 31;
+#pragma unroll
+        for (int it = 0; it < 5; it++) {
+            const int mid = (lo + hi) >> 1;
+            const int v = __shfl_sync(0xffffffffu, incl, mid);
+            if (v > idx)
+                hi = mid;
+            else
+                lo = mid + 1;
+        }
+        const int owner = lo;
+        int kth = idx - __shfl_sync(0xffffffffu, excl, owner);
+        const bool valid = idx < tot;
+        int pl = 0, qx = 0, qy = 0;
+        if (valid) {
+            for (int j = 0; j < KW; j++) {
+                const long long wi = first + (long long)owner * KW + j;
+                uint32_t w = __ldg(flags + wi);
+                const int c = __popc(w);
+                if (kth < c) {
+                    for (int i = 0; i < kth; i++)
+                        w &= w - 1;
+                    const int bit = __ffs(w) - 1;
+                    const long long row = wi / ww;
+                    qx = (int)(wi % ww) * 32 + (bit < 16 ? 2 * bit : 2 * (bit - 16) + 1);
+                    qy = (int)(row % ph);
+                    pl = (int)(row / ph);
+                    break;
+                }
+                kth -= c;
+            }
+        }
+        fn(pl, qx, qy, valid);
+    }
+}
+
+__global__ void __launch_bounds__(NT)
+k_round_decide(const CRAWKDenoise k, const CRAWKDenoiseExact e, const CRAWKDenoiseIO io, const CRAWKRound rd,
+               uint32_t *list, uint32_t list_cap, uint32_t *stats)
+{
+    __shared__ float Dw[NT / GA][WIN * WIN];
+    const int lane = threadIdx.x & 31, g = lane % GA;
+    float *D = Dw[threadIdx.x / GA];
+    const int ww = CRAW_K_ROUND_WW(k.pw);
+    const long long nwords = (long long)CRAW_K_ROUND_WORDS(k.pw, k.ph);
+    const long long gw = ((long long)blockIdx.x * NT + threadIdx.x) >> 5;
+    const long long nw = ((long long)gridDim.x * NT) >> 5;
+    for (long long first = gw * 32 * KW; first < nwords; first += nw * 32 * KW) {
+        walk_marks(rd.flags, nwords, ww, k.ph, first, lane, [&](int pl, int qx, int qy, bool valid) {
+            const uint32_t got = __ballot_sync(0xffffffffu, valid && g == 0);
+            if (lane == 0 && got)
+                atomicAdd(&stats[0], (uint32_t)__popc(got));
+            const bool done = decide(k, e, io, pl, qx, qy, valid, g, lane, D, stats);
+            if (valid && !done && g == 0) {
+                const uint32_t slot = atomicAdd(rd.count2, 1u);
+                if (slot < list_cap)
+                    list[slot] = ((uint32_t)pl * (uint32_t)k.ph + (uint32_t)qy) * (uint32_t)k.pw + (uint32_t)qx;
+            }
+        });
+    }
+}
+
+/* ------------------------------------------------ the double-float stage */
+
+CRAW_DEV dfl ld(const float v[2])
+{
+    return df_make(v[0], v[1]);
+}
+
+CRAW_DEV dfl shfl_df(dfl a, int m)
+{
+    return df_make(__shfl_xor_sync(0xffffffffu, a.hi, m), __shfl_xor_sync(0xffffffffu, a.lo, m));
+}
+
+/* The stabilised value of a raw code at quad site pl (reference
+ * lib/ref/ref_denoise.c:30-40 after the normalisation of 268-270). */
+CRAW_DEV dfl gat_fwd_x(const CRAWKDenoiseExact &e, uint32_t raw, int pl)
+{
+    const dfl r = df_mul_f(ld(e.inv65535), (float)raw);
+    const dfl u = df_mul(df_sub(r, ld(e.black[pl])), ld(e.inv_range[pl]));
+    if (u.hi >= 0.0f && !(u.hi == 0.0f && u.lo < 0.0f))
+        return df_mul(ld(e.gat_fwd), df_sqrt(df_add(df_mul_f(u, e.gat_a), ld(e.gat_c))));
+    return df_add(ld(e.gat_t0), df_mul(u, ld(e.gat_isc)));
+}
+
+/* The inverse (reference lib/ref/ref_denoise.c:44-58). */
+CRAW_DEV dfl gat_inv_x(const CRAWKDenoiseExact &e, dfl t)
+{
+    if (df_cmp(t, ld(e.gat_t0)) >= 0)
+        return df_sub(df_mul(df_mul(ld(e.gat_inv), t), t), ld(e.gat_off));
+    return df_mul(df_sub(t, ld(e.gat_t0)), ld(e.gat_sc));
+}
+
+/* The double evaluation's code of sample (pl, qx, qy), written to io.dst,
+ * by a group of G lanes (g = 0 .. G-1): each stabilises every G-th value
+ * of the window into the group's scratch (Th/Tl, 81 double-floats) and
+ * takes every G-th search offset; shuffles add the group's partial sums,
+ * and lane 0 of the group finishes. `valid` false: the lanes only take
+ * part in the synchronisation. */
+CRAW_DEV void exact_sample(const CRAWKDenoiseExact &e, const CRAWKDenoiseIO &io, int pl, int qx, int qy,
+                           bool valid, int g, float *Th, float *Tl, uint32_t *stats)
+{
+    const int px = pl & 1, py = pl >> 1;
+    if (valid) {
+        for (int s = g; s < WIN * WIN; s += G) {
+            const int yy = craw_mirror(qy + s / WIN - 4, e.ph), xx = craw_mirror(qx + s % WIN - 4, e.pw);
+            const dfl t = gat_fwd_x(e, row16(io.src, io.src_pitch, 2 * yy + py)[2 * xx + px], pl);
+            Th[s] = t.hi;
+            Tl[s] = t.lo;
+        }
+    }
+    __syncwarp();
+    dfl acc = df_from(0.0f), wsum = df_from(0.0f);
+    if (valid) {
+        for (int o = g; o < 49; o += G) {
+            const int dy = o / 7 - 3, dx = o % 7 - 3;
+            dfl d2 = df_from(0.0f);
+#pragma unroll
+            for (int ky = -1; ky <= 1; ky++)
+#pragma unroll
+                for (int kx = -1; kx <= 1; kx++) {
+                    const int a = (4 + ky) * WIN + 4 + kx, b = (4 + dy + ky) * WIN + 4 + dx + kx;
+                    const dfl d = df_sub(df_make(Th[a], Tl[a]), df_make(Th[b], Tl[b]));
+                    d2 = df_add_same(d2, df_sqr(d));
+                }
+            const dfl x = df_add_f(df_mul(d2, ld(e.k_nlm)), -2.0f);
+            const bool pos = x.hi > 0.0f || (x.hi == 0.0f && x.lo > 0.0f);
+            const dfl w = pos ? df_exp_neg(x) : df_from(1.0f);
+            const int c = (4 + dy) * WIN + 4 + dx;
+            acc = df_add(acc, df_mul(w, df_make(Th[c], Tl[c])));
+            wsum = df_add_same(wsum, w);
+        }
+    }
+#pragma unroll
+    for (int m = 1; m < G; m <<= 1) {
+        acc = df_add(acc, shfl_df(acc, m));
+        wsum = df_add_same(wsum, shfl_df(wsum, m));
+    }
+    __syncwarp();
+    if (!valid || g != 0)
+        return;
+    const dfl tm = df_div(acc, wsum);
+    dfl u = gat_inv_x(e, tm);
+    const int my = 2 * qy + py, mx = 2 * qx + px;
+    const uint16_t raw0 = row16(io.src, io.src_pitch, my)[mx];
+    const dfl u0 = df_mul(df_sub(df_mul_f(ld(e.inv65535), (float)raw0), ld(e.black[pl])), ld(e.inv_range[pl]));
+    const dfl gr = df_clamp01(df_mul(df_sub(u0, ld(e.guard_lo)), ld(e.guard_inv)));
+    u = df_add(u, df_mul(df_sub(u0, u), gr));
+    const dfl ro = df_clamp01(df_add(ld(e.black[pl]), df_mul(u, ld(e.range[pl]))));
+    const dfl xe = df_mul_f(ro, 65535.0f);
+    const float n = df_rint(xe);
+    const uint16_t code = (uint16_t)n;
+    uint16_t *cell = (uint16_t *)((char *)io.dst + (size_t)my * io.dst_pitch) + mx;
+    if (*cell != code) {
+        *cell = code;
+        record_change(stats, tm.hi, xe.hi, 0.5f - fabsf((xe.hi - n) + xe.lo), pl);
+    }
+}
+
+/* One group of G lanes a listed sample. */
+__global__ void __launch_bounds__(NT)
+k_round_exact(const CRAWKDenoiseExact e, const CRAWKDenoiseIO io, const CRAWKRound rd, const uint32_t *list,
+              uint32_t list_cap, uint32_t *stats)
+{
+    __shared__ float Th[NT / G][WIN * WIN], Tl[NT / G][WIN * WIN];
+    const uint32_t listed = *rd.count2, n = min(listed, list_cap);
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        atomicAdd(&stats[3], listed);
+    const int grp = threadIdx.x / G, g = threadIdx.x % G;
+    const uint32_t groups = gridDim.x * (NT / G);
+    /* Every lane runs the same number of rounds, so that the warp's
+     * synchronisations match. */
+    for (uint32_t base = blockIdx.x * (NT / G); base < n; base += groups) {
+        const uint32_t i = base + grp;
+        const bool valid = i < n;
+        const uint32_t v = valid ? list[i] : 0u;
+        const uint32_t qx = v % (uint32_t)e.pw, r = v / (uint32_t)e.pw;
+        exact_sample(e, io, (int)(r / (uint32_t)e.ph), (int)qx, (int)(r % (uint32_t)e.ph), valid, g, Th[grp],
+                     Tl[grp], stats);
+    }
+}
+
+} // namespace
+
+extern "C" int craw_k_denoise_round(const CRAWKDenoise *k, const CRAWKDenoiseExact *e, const CRAWKDenoiseIO *io,
+                                    const CRAWKRound *rd, uint32_t *list, uint32_t *stats, int sm_count,
+                                    cudaStream_t s)
+{
+    if (!k || !e || !io || !rd || !rd->flags || !rd->count2 || !list || !stats)
+        return -22;
+    if ((e->mode & (CRAW_K_DN_SPATIAL | CRAW_K_DN_TEMPORAL)) != CRAW_K_DN_SPATIAL)
+        return -22;
+    const int sms = sm_count > 0 ? sm_count : 152;
+    const size_t cap = CRAW_K_ROUND_LIST(k->pw, k->ph);
+    const long long steps = ((long long)CRAW_K_ROUND_WORDS(k->pw, k->ph) + 32 * KW - 1) / (32 * KW);
+    long long ctas_a = (steps + NT / 32 - 1) / (NT / 32);
+    ctas_a = ctas_a < (long long)sms * 8 ? ctas_a : (long long)sms * 8;
+    k_round_decide<<<(unsigned)(ctas_a > 0 ? ctas_a : 1), NT, 0, s>>>(*k, *e, *io, *rd, list, (uint32_t)cap, stats);
+    if (cudaGetLastError() != cudaSuccess)
+        return -5;
+    k_round_exact<<<(unsigned)sms * 8, NT, 0, s>>>(*e, *io, *rd, list, (uint32_t)cap, stats);
+    return cudaGetLastError() == cudaSuccess ? 0 : -5;
+}

@@ -347,9 +347,12 @@ struct SearchX2 {
 };
 
 /* One tile (tile column bx, tile row by) of all four planes; the whole
- * CTA takes part. `smem` holds Cfg::smem_floats floats. */
+ * CTA takes part. `smem` holds Cfg::smem_floats floats. `rd`: NULL, or
+ * the marking of samples whose code lies near a rounding boundary
+ * (CRAWKRound). */
 template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2 = false, bool STAGED = true>
-CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int bx, int by, float *smem)
+CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int bx, int by, float *smem,
+                           const CRAWKRound *rd = nullptr)
 {
     using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2, STAGED>;
     static_assert(!C::PACKED || BW == 2, "the packed search pairs a thread's two columns");
@@ -362,6 +365,8 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
 
     const int tx0 = bx * OX, ty0 = by * OY;
     const int tid = threadIdx.x;
+    if (rd && rd->count2 && bx == 0 && by == 0 && tid == 0)
+        *rd->count2 = 0;        /* this frame's list of undecided samples starts empty */
 
     /* ---- fill: the stabilised tile, temporally averaged when there is a
      * history (reference lib/ref/ref_denoise.c:244-296). */
@@ -498,12 +503,16 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
     /* This warp's plane constants, selected once (indexing the parameter
      * arrays with the warp's plane would copy them to local memory). */
     const float blk = pick4(k.black, pl), irng = pick4(k.inv_range, pl), rng = pick4(k.range, pl);
+    /* The marks need a half-warp's 16 lanes x BW columns to be one word. */
+    const bool mark = BW == 2 && rd && rd->flags;
 #pragma unroll
     for (int m = 0; m < M; m++) {
         const int qy = ty0 + oy0 + m;
+        bool near[BW];
 #pragma unroll
         for (int j = 0; j < BW; j++) {
             const int qx = tx0 + ox0 + j;
+            near[j] = false;
             if (qy >= k.ph || qx >= k.pw)
                 continue;
             const int my = 2 * qy + py, mx = 2 * qx + px;
@@ -533,11 +542,30 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
             float gr = fminf(fmaxf((u0 - k.guard_lo) * k.guard_inv, 0.0f), 1.0f);
             u = u + (u0 - u) * gr;
             float ro = fminf(fmaxf(blk + u * rng, 0.0f), 1.0f);
-            const uint16_t code = (uint16_t)rintf(ro * 65535.0f);
+            const float xv = ro * 65535.0f;
+            const uint16_t code = (uint16_t)rintf(xv);
+            if (mark) {
+                /* Within the float error of a rounding boundary: the exact
+                 * rounding decides this code. */
+                const float tm = SPATIAL ? res[m][j] : tc;
+                near[j] = fabsf(xv - rintf(xv)) > 0.5f - fmaf(tm * tm, rd->c2, rd->c0);
+            }
             if constexpr (STAGED)
                 *cell = code;
             else
                 ((uint16_t *)((char *)io.dst + (size_t)my * io.dst_pitch))[mx] = code;
+        }
+        if constexpr (BW == 2) {
+            if (mark) {
+                /* A half-warp holds one plane row's 32 columns tx0 .. tx0 + 31:
+                 * lane l's two columns are bits l and 16 + l of its word. */
+                const uint32_t b0 = __ballot_sync(0xffffffffu, near[0]);
+                const uint32_t b1 = __ballot_sync(0xffffffffu, near[1]);
+                const uint32_t sh = lane & 16;
+                const uint32_t word = ((b0 >> sh) & 0xffffu) | (((b1 >> sh) & 0xffffu) << 16);
+                if ((lane & 15) == 0 && qy < k.ph)
+                    rd->flags[((size_t)pl * k.ph + qy) * CRAW_K_ROUND_WW(k.pw) + (tx0 >> 5)] = word;
+            }
         }
     }
     if constexpr (!STAGED)
