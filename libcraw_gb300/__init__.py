@@ -56,6 +56,7 @@ FLAG_SHARPEN = 1 << 8
 FLAG_PROFILE = 1 << 9
 FLAG_KEEP_INTERMEDIATE = 1 << 16
 FLAG_NO_AUTOTUNE = 1 << 17
+FLAG_EXACT_ROUNDING = 1 << 18
 BATCH_FLAG_UNFUSED = 1 << 20
 BATCH_FLAG_NO_GRAPH = 1 << 21
 BATCH_FLAG_FUSED = 1 << 22

@@ -495,7 +495,7 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
     }
     if ((ret = craw_dev_alloc(ctx, (void **)&p->kerr, 16)) < 0)
         goto fail;
-    if (p->has_denoise && !p->plain) {
+    if (p->has_denoise && !p->plain && (params->flags & CRAW_PIPELINE_FLAG_EXACT_ROUNDING)) {
         /* The exact rounding: its marks (a bit per sample, 2.3 MB at
          * 5760x3240), the list of samples its float stage cannot settle
          * (a sixteenth of the samples and their count: 4.9 MB) and its

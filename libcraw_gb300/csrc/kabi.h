@@ -63,8 +63,9 @@ enum CRAWKDenoiseShape {
  * as the double evaluation rounds them. */
 typedef struct CRAWKRound {
     uint32_t *flags;    /* CRAW_K_ROUND_WORDS(pw, ph) words; NULL: no marking */
-    uint32_t *count2;   /* the length of the list of undecided samples: the
-                         * denoise kernel zeroes it */
+    uint32_t *count2;   /* [0] the length of the list of undecided samples,
+                         * [1] the rounding's work counter: the denoise
+                         * kernel zeroes both */
     float c0, c2;
 } CRAWKRound;
 

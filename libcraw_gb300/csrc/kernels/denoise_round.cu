@@ -45,9 +45,9 @@ namespace {
 
 constexpr int NT = 128;                /* threads per CTA */
 constexpr int WIN = 9;                 /* search 3 + patch 1, both sides */
-constexpr int KW = 4;                  /* bit-map words a lane scans a step */
+constexpr int KW = 1;                  /* bit-map words a lane scans a step */
 constexpr int GA = 4;                  /* lanes of the decision stage a sample */
-constexpr int G = 8;                   /* lanes of the exact stage a sample */
+constexpr int G = 32;                  /* lanes of the exact stage a sample */
 constexpr float U = 0x1p-24f;          /* float unit roundoff */
 
 /* ------------------------------------------------------------ helpers */
@@ -275,9 +275,16 @@ k_round_decide(const CRAWKDenoise k, const CRAWKDenoiseExact e, const CRAWKDenoi
     float *D = Dw[threadIdx.x / GA];
     const int ww = CRAW_K_ROUND_WW(k.pw);
     const long long nwords = (long long)CRAW_K_ROUND_WORDS(k.pw, k.ph);
-    const long long gw = ((long long)blockIdx.x * NT + threadIdx.x) >> 5;
-    const long long nw = ((long long)gridDim.x * NT) >> 5;
-    for (long long first = gw * 32 * KW; first < nwords; first += nw * 32 * KW) {
+    /* Warps take steps of 32 KW words off a shared counter: the marks
+     * gather where the image is bright, so fixed shares would leave a few
+     * warps with most of the work. */
+    for (;;) {
+        uint32_t step = 0;
+        if (lane == 0)
+            step = atomicAdd(rd.count2 + 1, 1u);
+        const long long first = (long long)__shfl_sync(0xffffffffu, step, 0) * 32 * KW;
+        if (first >= nwords)
+            break;
         walk_marks(rd.flags, nwords, ww, k.ph, first, lane, [&](int pl, int qx, int qy, bool valid) {
             const uint32_t got = __ballot_sync(0xffffffffu, valid && g == 0);
             if (lane == 0 && got)
@@ -426,7 +433,7 @@ extern "C" int craw_k_denoise_round(const CRAWKDenoise *k, const CRAWKDenoiseExa
     const size_t cap = CRAW_K_ROUND_LIST(k->pw, k->ph);
     const long long steps = ((long long)CRAW_K_ROUND_WORDS(k->pw, k->ph) + 32 * KW - 1) / (32 * KW);
     long long ctas_a = (steps + NT / 32 - 1) / (NT / 32);
-    ctas_a = ctas_a < (long long)sms * 8 ? ctas_a : (long long)sms * 8;
+    ctas_a = ctas_a < (long long)sms * 12 ? ctas_a : (long long)sms * 12;
     k_round_decide<<<(unsigned)(ctas_a > 0 ? ctas_a : 1), NT, 0, s>>>(*k, *e, *io, *rd, list, (uint32_t)cap, stats);
     if (cudaGetLastError() != cudaSuccess)
         return -5;

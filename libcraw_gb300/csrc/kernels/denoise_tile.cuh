@@ -365,8 +365,10 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
 
     const int tx0 = bx * OX, ty0 = by * OY;
     const int tid = threadIdx.x;
-    if (rd && rd->count2 && bx == 0 && by == 0 && tid == 0)
-        *rd->count2 = 0;        /* this frame's list of undecided samples starts empty */
+    if (rd && rd->count2 && bx == 0 && by == 0 && tid == 0) {
+        rd->count2[0] = 0;      /* this frame's list of undecided samples starts empty */
+        rd->count2[1] = 0;      /* and so does the rounding's work counter */
+    }
 
     /* ---- fill: the stabilised tile, temporally averaged when there is a
      * history (reference lib/ref/ref_denoise.c:244-296). */

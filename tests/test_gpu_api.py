@@ -206,7 +206,7 @@ def test_stage_times(ctx):
         develop(pipe, m, fp)
         st = pipe.stage_times()
         names = [s[0] for s in st]
-        assert names == ["denoise_nlm", "denoise_round", "develop", "awb_reduce"], names
+        assert names == ["denoise_nlm", "develop", "awb_reduce"], names
         assert all(s[1] == 1 and s[2] > 0 for s in st)
     with L.Pipeline(ctx, L.pipeline_params(w, h)) as pipe:
         with pytest.raises(L.CrawError) as e:

@@ -42,8 +42,8 @@ def _default_rounding():
 def denoise_gpu(ctx, m, prof, model, strength):
     """(denoised mosaic, round statistics) of one record."""
     h, w = m.shape
-    pp = L.pipeline_params(w, h, flags=L.FLAG_DENOISE | L.FLAG_KEEP_INTERMEDIATE, out_format=L.FORMAT_RGBA32F,
-                           out_space=L.CS_ACES_AP1)
+    pp = L.pipeline_params(w, h, flags=L.FLAG_DENOISE | L.FLAG_KEEP_INTERMEDIATE | L.FLAG_EXACT_ROUNDING,
+                           out_format=L.FORMAT_RGBA32F, out_space=L.CS_ACES_AP1)
     fp = L.frame_params(prof, denoise_strength=strength, noise_override=model)
     with L.Pipeline(ctx, pp) as pipe:
         pipe.round_stats()
@@ -122,7 +122,8 @@ def test_headline_chain_within_1e3_of_fp64(ctx, deb):
     c = W.workload("nlm_rcd_ap1", w, h)
     m = c.frame()
     prof = W.make_profile()
-    pp = L.pipeline_params(w, h, debayer=deb, out_space=c.out_space, flags=c.flags | L.FLAG_KEEP_INTERMEDIATE,
+    pp = L.pipeline_params(w, h, debayer=deb, out_space=c.out_space,
+                           flags=c.flags | L.FLAG_KEEP_INTERMEDIATE | L.FLAG_EXACT_ROUNDING,
                            out_format=L.FORMAT_RGBA32F)
     fp = L.frame_params(prof, **c.frame_kwargs())
     with L.Pipeline(ctx, pp) as pipe:

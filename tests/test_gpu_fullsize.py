@@ -17,7 +17,14 @@ do not need the oracle to develop the whole frame:
     GPU left (the temporal agreement test reads one plane sample around a
     pixel, the NLM four, well inside the margin);
   * the 16-frame batch mix at its real sizes (168 Mpx) in one batch
-    record against each frame's own single-frame pipeline.
+    record against each frame's own single-frame pipeline;
+  * against the FP64 oracle: the default (float) rounding of the denoised
+    codes differs from the double evaluation's at no more samples than the
+    reference's own float code does, and the develop stage alone (the FP64
+    develop of the GPU's own denoised mosaic) is within 1e-3; with
+    CRAW_PIPELINE_FLAG_EXACT_ROUNDING the denoised mosaic is the double
+    evaluation's code for code and the developed frame within 1e-3 of the
+    FP64 chain.
 """
 import numpy as np
 import pytest
@@ -26,7 +33,7 @@ import torch
 import libcraw_gb300 as L
 from libcraw_gb300 import workloads as W
 from gpu_util import alloc_rgba, download_image, upload_mosaic
-from oracle import Oracle, denoised_chain_ok
+from oracle import Oracle, denoised_chain_ok, max_rel
 
 pytestmark = pytest.mark.gpu
 
@@ -73,11 +80,85 @@ def developed():
             out, dst = alloc_rgba(WIDTH, HEIGHT)
             pipe.record(s, src, dst, fp)
             torch.cuda.synchronize()
-            rgb_img, _ = pipe.intermediate()
+            rgb_img, mos_img = pipe.intermediate()
             res["rgb"] = download_image(rgb_img, "rgba32f").astype(np.float32)
+            res["mosaic"] = download_image(mos_img, "r16").copy()
             res["hist_keep"] = pipe.awb_histogram()
             res["same_keep"] = bool(np.array_equal(out.cpu().numpy(), res["got"]))
+            del out
+        pp.flags |= L.FLAG_EXACT_ROUNDING
+        with L.Pipeline(ctx, pp) as pipe:
+            out, dst = alloc_rgba(WIDTH, HEIGHT)
+            pipe.record(s, src, dst, fp)
+            torch.cuda.synchronize()
+            _, mos_img = pipe.intermediate()
+            res["mosaic_exact"] = download_image(mos_img, "r16").copy()
+            res["got_exact"] = out.cpu().numpy()
     return res
+
+
+def _crop(win):
+    x, y, w, h = win
+    x0, y0 = max(0, x - MARGIN), max(0, y - MARGIN)
+    x1, y1 = min(WIDTH, x + w + MARGIN), min(HEIGHT, y + h + MARGIN)
+    return x0, y0, x1, y1
+
+
+@pytest.fixture(scope="module")
+def fp64_windows(developed):
+    """Per window: the FP64 and float oracle denoised mosaics of the crop,
+    the FP64 chain, and the FP64 develop of the GPU's own denoised mosaic."""
+    c, m, fp = developed["c"], developed["m"], developed["fp"]
+    model = (fp.noise_override.a, fp.noise_override.b)
+    out = []
+    for win in WINDOWS:
+        x, y, w, h = win
+        x0, y0, x1, y1 = _crop(win)
+        crop = np.ascontiguousarray(m[y0:y1, x0:x1])
+        sl = (slice(y - y0, y - y0 + h), slice(x - x0, x - x0 + w))
+        d64, _ = orc.denoise_temporal(crop, fp.profile.contents, model, fp.denoise_strength, 0.0, s="f64")
+        d32, _ = orc.denoise_temporal(crop, fp.profile.contents, model, fp.denoise_strength, 0.0, s="f32")
+        pp = L.pipeline_params(x1 - x0, y1 - y0, debayer=c.debayer, out_space=c.out_space, flags=c.flags,
+                               out_format=L.FORMAT_RGBA32F)
+        chain64 = orc.process(crop, pp, fp, "f64")[sl]
+        pp0 = L.pipeline_params(x1 - x0, y1 - y0, debayer=c.debayer, out_space=c.out_space,
+                                out_format=L.FORMAT_RGBA32F)
+        gmos = np.ascontiguousarray(developed["mosaic"][y0:y1, x0:x1])
+        dev64 = orc.process(gmos, pp0, L.frame_params(fp.profile.contents), "f64")[sl]
+        out.append(dict(win=win, sl=sl, d64=d64[sl], d32=d32[sl], chain64=chain64, dev64=dev64))
+    return out
+
+
+def test_default_rounding_vs_fp64(developed, fp64_windows):
+    """The default float path: its denoised codes differ from the double
+    evaluation's at no more samples than the reference's own float code's
+    do (both are one-code flips at values within float error of a
+    rounding boundary), and the develop stage on its own mosaic is within
+    1e-3 of FP64."""
+    gpu_flips = ref_flips = total = 0
+    for wv in fp64_windows:
+        x, y, w, h = wv["win"]
+        g = developed["mosaic"][y:y + h, x:x + w]
+        d = np.abs(g.astype(np.int32) - wv["d64"].astype(np.int32))
+        assert d.max() <= 1, wv["win"]
+        gpu_flips += int((d > 0).sum())
+        ref_flips += int((wv["d32"] != wv["d64"]).sum())
+        total += w * h
+        got = developed["got"][y:y + h, x:x + w]
+        assert max_rel(got, wv["dev64"]) <= 1e-3, (wv["win"], max_rel(got, wv["dev64"]))
+    print(f"code flips against FP64 in {total} samples: GPU float path {gpu_flips}, reference float {ref_flips}")
+    assert gpu_flips <= ref_flips, (gpu_flips, ref_flips)
+
+
+def test_exact_rounding_vs_fp64(developed, fp64_windows):
+    """CRAW_PIPELINE_FLAG_EXACT_ROUNDING: the denoised mosaic is the FP64
+    oracle's code for code, and the developed frame within 1e-3 of the
+    FP64 chain, in every window (corners, edges, centre) at 5760x3240."""
+    for wv in fp64_windows:
+        x, y, w, h = wv["win"]
+        assert np.array_equal(developed["mosaic_exact"][y:y + h, x:x + w], wv["d64"]), wv["win"]
+        got = developed["got_exact"][y:y + h, x:x + w]
+        assert max_rel(got, wv["chain64"]) <= 1e-3, (wv["win"], max_rel(got, wv["chain64"]))
 
 
 @pytest.mark.parametrize("win", WINDOWS, ids=[f"{x}_{y}" for x, y, _, _ in WINDOWS])
