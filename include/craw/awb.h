@@ -145,12 +145,11 @@ CRAW_API int craw_awb_smoother_push(CRAWAwbSmoother *sm, double pts_s,
  * This entry point has no counterpart in the reference.
  *
  * Who needs it: a caller that must not allocate device memory at the
- * moment it wants the statistic. A thread that runs while another thread
- * of the process captures a CUDA graph in global mode, where a cudaMalloc
- * would invalidate that capture; a serving loop that has handed its whole
+ * moment it wants the statistic. A serving loop that has handed its whole
  * device-memory budget to the streams it admitted; a latency-bound thread
  * that cannot afford the device-wide synchronisation a fresh allocation
- * may cause. The pipeline's own AWB pass gets its scratch from memory it
+ * may cause; code that runs under an allocator it does not own, which may
+ * refuse or reorder a request made at that moment. The pipeline's own AWB pass gets its scratch from memory it
  * allocates at creation; this one uses a fixed array in the library's
  * device image instead (3.3 MB per device, present once the library's
  * module is loaded there).
@@ -167,7 +166,13 @@ CRAW_API int craw_awb_smoother_push(CRAWAwbSmoother *sm, double pts_s,
  *    with CRAW_ERROR(EINVAL) and a log line, before any device work;
  *  - the first call on each device does the set-up: it looks up the device
  *    address of the scratch array (cudaGetSymbolAddress, with that device
- *    current). Make that first call before any stream capture begins;
+ *    current) and keeps it for the process (a failed lookup is retried on
+ *    the next call). Make that first call before any stream capture
+ *    begins. A cudaDeviceReset() (or any other teardown of the device's
+ *    primary context) leaves the kept address stale: do not call this
+ *    entry point on a device after resetting it;
+ *  - a CUDA error that an earlier call left pending on the calling thread
+ *    is reported (CRAW_ERROR(EIO)), not cleared;
  *  - the histograms and the counter in the scratch must be zero when the
  *    kernel starts; each call clears them on `stream` itself first;
  *  - all calls on one device share the one scratch array: two calls that

@@ -315,7 +315,8 @@ CRAW_API int craw_noise_estimate_cuda(const CRAWImage *mosaic, const CRAWProfile
     if (mosaic->format != CRAW_FORMAT_R16_UNORM || !mosaic->data || ((uintptr_t)mosaic->data & 15) ||
         (mosaic->pitch & 15) || mosaic->pitch < (size_t)mosaic->width * 2)
         return CRAW_ERROR(EINVAL);
-    (void)cudaGetLastError();
+    if (cudaPeekAtLastError() != cudaSuccess)
+        return CRAW_ERROR(EIO);         /* the caller's pending error is not ours to clear */
     return ne_run(&k, mosaic->data, mosaic->pitch, min_n, profile, out, stream);
 }
 
@@ -336,7 +337,8 @@ CRAW_API int craw_noise_estimate(const uint16_t *bayer, uint32_t width, uint32_t
         return ret;
     if (stride < width)
         return CRAW_ERROR(EINVAL);
-    (void)cudaGetLastError();
+    if (cudaPeekAtLastError() != cudaSuccess)
+        return CRAW_ERROR(EIO);         /* the caller's pending error is not ours to clear */
     if ((ret = ne_cuda_err(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking))) < 0)
         return ret == CRAW_ERROR(ENOMEM) ? ret : CRAW_ERROR(EIO);
     if ((ret = ne_cuda_err(cudaMallocAsync(&frame, pitch * height, s))) < 0) {

@@ -846,7 +846,7 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
 launch_fail:
     /* A launch CUDA refused: the stream may hold part of this recording,
      * so the temporal state is forgotten rather than trusted. */
-    craw_log(ctx, CRAW_LOG_ERROR, "Kernel launch failed: %s\n", cudaGetErrorString(cudaGetLastError()));
+    craw_log(ctx, CRAW_LOG_ERROR, "Kernel launch failed (%s)\n", cudaGetErrorString(cudaPeekAtLastError()));
     p->tn_prev = p->tn_cur = -1;
     return CRAW_ERROR(EIO);
 }

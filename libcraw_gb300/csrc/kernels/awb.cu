@@ -58,7 +58,8 @@ k_awb_reduce(const uint64_t *__restrict__ rec, uint32_t n, uint32_t *__restrict_
 
 extern "C" int craw_k_awb_reduce(const uint64_t *rec, uint32_t n, uint32_t *hist, cudaStream_t s)
 {
-    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
+    if (craw_launch_ready() < 0)
+        return -5;
     static std::atomic<uint64_t> attr_done{ 0 };
     const int smem = 3 * kBins * (int)sizeof(uint32_t);
     if (craw_smem_attr(k_awb_reduce, (size_t)smem, attr_done) < 0)

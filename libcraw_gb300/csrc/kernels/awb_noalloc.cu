@@ -115,27 +115,29 @@ k_awb_noalloc(const float *rgb, int w, int h, size_t stride, int ch, float wb0, 
     atomicAdd(&sc[2 * kBins2 + bin], bq);
 }
 
-/* The scratch's device address, looked up once per device. */
+/* The scratch's device address, looked up on the first call on each
+ * device (cudaGetSymbolAddress with that device current) and kept; a
+ * lookup that fails is not kept, so the next call tries again. */
 constexpr int kMaxDevices = 64;
-std::once_flag setup_once[kMaxDevices];
+std::mutex setup_lock;
 uint32_t *setup_ptr[kMaxDevices];
-cudaError_t setup_err[kMaxDevices];
 
 int scratch_address(uint32_t **out)
 {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return CRAW_ERROR(ENODEV);
-    std::call_once(setup_once[dev], [dev] {
-        void *p = nullptr;
-        setup_err[dev] = cudaGetSymbolAddress(&p, awb_noalloc_scratch);
-        setup_ptr[dev] = setup_err[dev] == cudaSuccess ? static_cast<uint32_t *>(p) : nullptr;
-    });
+    std::lock_guard<std::mutex> lock(setup_lock);
     if (!setup_ptr[dev]) {
-        craw_log(NULL, CRAW_LOG_ERROR, "craw_awb_histogram_from_rgb_cuda_noalloc: "
-                 "cudaGetSymbolAddress failed on device %d: %s\n", dev,
-                 cudaGetErrorString(setup_err[dev]));
-        return CRAW_ERROR(EIO);
+        void *p = nullptr;
+        const cudaError_t err = cudaGetSymbolAddress(&p, awb_noalloc_scratch);
+        if (err != cudaSuccess) {
+            (void)cudaGetLastError();   /* this lookup's own error */
+            craw_log(NULL, CRAW_LOG_ERROR, "craw_awb_histogram_from_rgb_cuda_noalloc: "
+                     "cudaGetSymbolAddress failed on device %d: %s\n", dev, cudaGetErrorString(err));
+            return CRAW_ERROR(EIO);
+        }
+        setup_ptr[dev] = static_cast<uint32_t *>(p);
     }
     *out = setup_ptr[dev];
     return 0;
@@ -165,7 +167,12 @@ extern "C" CRAW_API int craw_awb_histogram_from_rgb_cuda_noalloc(
                  (unsigned long long)blocks, kMaxBlocks);
         return CRAW_ERROR(EINVAL);
     }
-    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
+    if (cudaPeekAtLastError() != cudaSuccess) {
+        /* An error an earlier call left pending: the caller's to read. */
+        craw_log(NULL, CRAW_LOG_ERROR, "craw_awb_histogram_from_rgb_cuda_noalloc: a CUDA error of an "
+                 "earlier call is pending (%s)\n", cudaGetErrorString(cudaPeekAtLastError()));
+        return CRAW_ERROR(EIO);
+    }
     if ((ret = scratch_address(&sc)) < 0)
         return ret;
     if (cudaMemsetAsync(sc, 0, (kCounter + 1) * sizeof(uint32_t), stream) != cudaSuccess)

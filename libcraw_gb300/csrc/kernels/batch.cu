@@ -213,7 +213,8 @@ extern "C" void craw_k_batch_tiles(int32_t w, int32_t h, int shape, int32_t *dn_
 extern "C" int craw_k_batch(const CRAWKBatchTable *table, int32_t nb, int32_t dn_items,
                             int32_t dv_items, int method, int shape, int fused, cudaStream_t s)
 {
-    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
+    if (craw_launch_ready() < 0)
+        return -5;
     if (nb <= 0 || nb > CRAW_K_BATCH_MAX)
         return -22;
     switch (shape) {

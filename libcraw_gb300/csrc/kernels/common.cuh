@@ -13,6 +13,15 @@
 
 #define CRAW_DEV __device__ __forceinline__
 
+/* 0, or -5 (EIO) when a CUDA error of an earlier call is pending on this
+ * thread: it is the caller's to read, not ours to clear, and a launch now
+ * could not tell its own error from it. Every launcher checks this first,
+ * then reads (and so clears) only the error of its own launches. */
+inline int craw_launch_ready()
+{
+    return cudaPeekAtLastError() == cudaSuccess ? 0 : -5;
+}
+
 /* Lets `fn` take `bytes` of dynamic shared memory, once per device (the
  * attribute belongs to the function in each device's context); `done`
  * holds a bit per device ordinal below 64, above which it is set every

@@ -53,7 +53,8 @@ int dispatch(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, const CRAWKRound *
 extern "C" int craw_k_denoise(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, int shape,
                               const CRAWKRound *rd, cudaStream_t s)
 {
-    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
+    if (craw_launch_ready() < 0)
+        return -5;
     switch (shape) {
     case CRAW_K_DN_SHAPE_2x8:    return dispatch<2, 8, 1, false>(k, io, rd, s);
     case CRAW_K_DN_SHAPE_2x4:    return dispatch<2, 4, 2, false>(k, io, rd, s);

@@ -429,6 +429,8 @@ extern "C" int craw_k_denoise_round(const CRAWKDenoise *k, const CRAWKDenoiseExa
         return -22;
     if ((e->mode & (CRAW_K_DN_SPATIAL | CRAW_K_DN_TEMPORAL)) != CRAW_K_DN_SPATIAL)
         return -22;
+    if (craw_launch_ready() < 0)
+        return -5;
     const int sms = sm_count > 0 ? sm_count : 152;
     const size_t cap = CRAW_K_ROUND_LIST(k->pw, k->ph);
     const long long steps = ((long long)CRAW_K_ROUND_WORDS(k->pw, k->ph) + 32 * KW - 1) / (32 * KW);

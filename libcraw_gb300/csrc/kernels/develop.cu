@@ -257,7 +257,8 @@ int launch_rcd(const CRAWKDevelop *k, const CRAWKDevelopIO *io, cudaStream_t s)
 extern "C" int craw_k_develop(const CRAWKDevelop *k, const CRAWKDevelopIO *io, int shape,
                               cudaStream_t s)
 {
-    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
+    if (craw_launch_ready() < 0)
+        return -5;
     (void)shape;
     switch (k->method) {
     case kBilinear: return launch<kBilinear, 64, 16, 256>(k, io, s);

@@ -481,7 +481,8 @@ extern "C" int64_t craw_k_highlight_levels(int32_t width, int32_t height, CRAWKH
 
 extern "C" int craw_k_highlights(const CRAWKHighlight *k, const CRAWKHighlightIO *io, cudaStream_t s)
 {
-    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
+    if (craw_launch_ready() < 0)
+        return -5;
     const int qw = k->width / 2, qh = k->height / 2;
     const dim3 blk(32, 8);
     k_hl_level0<<<dim3((k->lw[0] + kF0W - 1) / kF0W, (k->lh[0] + kF0H - 1) / kF0H), kF0Threads, 0, s>>>(

@@ -345,7 +345,8 @@ extern "C" size_t craw_k_noise_scratch(int32_t width, int32_t height, int32_t nb
 extern "C" int craw_k_noise_bins(const CRAWKNoise *k, const uint16_t *src, size_t src_pitch, void *scratch,
                                  CRAWKNoiseBin *bins, cudaStream_t s)
 {
-    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
+    if (craw_launch_ready() < 0)
+        return -5;
     const Layout L = layout(k->width, k->height, k->nb_bins);
     char *base = static_cast<char *>(scratch);
     float *lut = reinterpret_cast<float *>(base + L.lut);
@@ -376,7 +377,8 @@ extern "C" int craw_k_noise_bins(const CRAWKNoise *k, const uint16_t *src, size_
 extern "C" int craw_k_noise_lts(const double *m, const double *v, const double *lv, int32_t nb, int32_t keep,
                                 double *cost, cudaStream_t s)
 {
-    (void)cudaGetLastError();
+    if (craw_launch_ready() < 0)
+        return -5;
     if (nb < 2 || nb > CRAW_K_NOISE_MAX_BINS)
         return -22;
     int np2 = 32;

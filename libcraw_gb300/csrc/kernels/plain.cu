@@ -442,7 +442,8 @@ __global__ void p_color(const CRAWKDevelop k, const float *inter, size_t ip, voi
 extern "C" int craw_k_plain_denoise(const CRAWKDenoise *k, const CRAWKDenoiseIO *io,
                                     float *t, float *var, cudaStream_t s)
 {
-    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
+    if (craw_launch_ready() < 0)
+        return -5;
     dim3 g(((k->pw + B2 - 1) / B2), (k->ph + B2 - 1) / B2, 4), b(B2, B2);
     const size_t plane = (size_t)4 * k->pw * k->ph;
     if (k->mode & CRAW_K_DN_HISTORY) {
@@ -462,7 +463,8 @@ extern "C" int craw_k_plain_develop(const CRAWKDevelop *k, const CRAWKDevelopIO 
                                     size_t ip, float *scratch, float *q, float *qf,
                                     uint32_t *hist, cudaStream_t s)
 {
-    (void)cudaGetLastError();   /* a stale error of an earlier call is not ours */
+    if (craw_launch_ready() < 0)
+        return -5;
     const int w = k->width, h = k->height;
     const size_t n = (size_t)w * h;
     p_prep<<<GRID2(w, h), 0, s>>>(*k, io->src, io->src_pitch, v);
