@@ -33,7 +33,9 @@ ORACLE = ROOT / "oracle"
 CUDA_HOME = Path(os.environ.get("CUDA_HOME", "/usr/local/cuda"))
 NVCC = str(CUDA_HOME / "bin" / "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-REFERENCE = Path("/root/reference")
+#: The reference's source tree, where present (it is not on every machine
+#: that builds this project): CRAW_REFERENCE_DIR, else its usual checkout.
+REFERENCE = Path(os.environ.get("CRAW_REFERENCE_DIR", "/root/reference"))
 
 HOST_CFLAGS = ["-std=c2x", "-O2", "-fPIC", "-fvisibility=hidden", "-Wall", "-Wextra",
                "-Wno-unused-parameter", "-Wno-missing-field-initializers",
@@ -111,7 +113,10 @@ def build(verbose: bool = False, with_reference: bool | None = None) -> dict[str
     orc_src = ORACLE / "craw_oracle.c"
     orc = ORACLE / "_build" / "liboracle.so"
     if _stale(orc, [orc_src, ORACLE / "oracle_impl.h", ORACLE / "craw_oracle.h"], hdr):
-        _run(["gcc", "-std=c2x", "-O2", "-fPIC", "-ffp-contract=off", "-shared",
+        # -O3: the CPU baseline (bench.py) times this build; -ffp-contract=off
+        # keeps its float results those of the reference's build on every host
+        # (no -march=native: the same results on the x86 and Arm machines).
+        _run(["gcc", "-std=c2x", "-O3", "-fPIC", "-ffp-contract=off", "-shared",
               "-fvisibility=hidden", f"-I{ROOT / 'include'}", f"-I{CUDA_HOME / 'include'}",
               str(orc_src), "-o", str(orc), "-lm"])
 

@@ -9,9 +9,10 @@
 # Also builds and runs the reference's own CPU unit tests (test_ref_debayer,
 # test_awb) against it, which is the check that the build is the reference.
 #
-#   usage: oracle/build_ref.sh [REFERENCE_DIR]   (default /root/reference)
+#   usage: oracle/build_ref.sh [REFERENCE_DIR]
+#   (default: $CRAW_REFERENCE_DIR, else /root/reference)
 set -eu
-REF=${1:-/root/reference}
+REF=${1:-${CRAW_REFERENCE_DIR:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 [ -d "$REF/lib/ref" ] || { echo "reference tree not found at $REF" >&2; exit 1; }

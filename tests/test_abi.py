@@ -8,9 +8,10 @@ from pathlib import Path
 import pytest
 
 import libcraw_gb300 as L
+from libcraw_gb300.build import REFERENCE
 
 ROOT = Path(__file__).resolve().parent.parent
-REF_INCLUDE = Path("/root/reference/include")
+REF_INCLUDE = REFERENCE / "include"
 
 
 def declared_symbols():
