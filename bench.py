@@ -69,7 +69,7 @@ def parse():
                          "(CRAW_PIPELINE_FLAG_EXACT_ROUNDING), which the metric's 1e-3 bound needs; "
                          "float: the reference's float rounding")
     ap.add_argument("--no-extras", action="store_true", help="skip the plain/fp16/cpu side runs")
-    ap.add_argument("--extras", default="plain,fp16,batch,temporal,serve,highlights,noise,cpu",
+    ap.add_argument("--extras", default="plain,fp16,batch,temporal,serve,target,config1,highlights,noise,cpu",
                     help="comma list of side runs: plain, fp16, batch, temporal, serve, highlights, "
                          "noise, cpu")
     ap.add_argument("--force-shape", type=int, default=-1,
@@ -516,6 +516,10 @@ def run_gpu(args):
             if base:
                 extras["serve"]["eq_speedup_vs_plain_fp32"] = (
                     extras["serve"]["saturated"]["eq_5760x3240_fps"] / base)
+        if "target" in want:
+            extras["target"] = run_target(ctx, stream)
+        if "config1" in want:
+            extras["config1"] = run_config1(ctx, stream, max(10, args.steps), 3)
         if "highlights" in want:
             extras["highlights"] = run_highlights(ctx, stream)
         if "noise" in want:
@@ -737,6 +741,45 @@ def run_noise_estimate(nsteps: int = 10, cpu: bool = True) -> dict:
     return res
 
 
+def run_config1(ctx, stream, steps: int, warmup: int) -> dict:
+    """The plain-method configuration: one 1920x1080 frame, bilinear, no
+    denoise, BT.709 linear float32 + AWB histogram, from device memory, L2
+    flushed between steps (the frame and its output fit in it)."""
+    import torch
+    import libcraw_gb300 as L
+    from libcraw_gb300 import workloads as W
+
+    c = W.workload("bilinear_bt709_1080p")
+    w, h = c.width, c.height
+    fp = L.frame_params(W.make_profile())
+    frames = [torch.from_numpy(W.synth_frame(w, h, c.seed + i, rects=c.rects, zone_plates=c.zone_plates,
+                                             noise_a_dn=c.noise_a_dn, noise_b_dn=c.noise_b_dn).view(np.int16)).cuda()
+              for i in range(4)]
+    srcs = [L.Image(t.data_ptr(), w * 2, L.FORMAT_R16_UNORM, w, h) for t in frames]
+    out = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    dst = L.Image(out.data_ptr(), w * 16, L.FORMAT_RGBA32F, w, h)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    pp = L.pipeline_params(w, h, debayer=c.debayer, out_space=c.out_space, flags=c.flags,
+                           out_format=L.FORMAT_RGBA32F)
+    sptr = stream.cuda_stream
+    with L.Pipeline(ctx, pp) as pipe, torch.cuda.stream(stream):
+        for i in range(warmup):
+            pipe.record(sptr, srcs[i % 4], dst, fp)
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for i, (e0, e1) in enumerate(evs):
+            flush.zero_()
+            e0.record(stream)
+            pipe.record(sptr, srcs[i % 4], dst, fp)
+            e1.record(stream)
+        torch.cuda.synchronize()
+    ms = [a.elapsed_time(b) for a, b in evs]
+    # Algorithmic bytes: mosaic in 2 B/px, RGBA32F out 16 B/px, AWB records 8 B per 64 px.
+    gbs = (18.0 + 8.0 / 64) * w * h / (statistics.mean(ms) / 1000.0) / 1e9
+    return {"workload": "1920x1080 RGGB 12-bit (var = 2 s + 16 DN^2): bilinear, no denoise, BT.709 f32 + AWB",
+            "fps": 1000.0 / statistics.mean(ms), "ms_per_frame": statistics.mean(ms),
+            "hbm_gbs": gbs, "hbm_frac": gbs / peaks()["hbm_gbs"]}
+
+
 def run_temporal_seq(ctx, stream, nsteps: int = 60, distinct: int = 12) -> dict:
     """The temporal sequence (60 frames of 5760x3240, rectangles moving 2, 8
     and 24 px/frame, temporal 0.8 + NLM 1.0 + chroma 0.5 + MHC + P3-D65
@@ -789,6 +832,119 @@ def run_temporal_seq(ctx, stream, nsteps: int = 60, distinct: int = 12) -> dict:
                                       "psnr_db": 10 * np.log10(peak * peak / max(mse, 1e-30))}
     res["workload"] = (f"{w}x{h} x{nsteps} (12 distinct seeded frames cycled), movers 2/8/24 px: "
                        "temporal 0.8 + NLM 1.0 + chroma 0.5 + MHC + P3-D65 f32 + AWB")
+    return res
+
+
+def run_target(ctx, stream, nframes: int = 24, plain_frames: int = 6, streams: int = 4) -> dict:
+    """The headline target's chain: 5760x3240 frames through temporal 0.8 +
+    NLM 1.0 + RCD + matrix (ACES AP1, RGC) float32, FP16 storage, against
+    the plain FP32 single-frame pipeline on the same chain, temporal
+    included. Frames/s of: the plain FP32 pipeline; the fused FP16 pipeline
+    (device-resident frames, CUDA events); the frame server developing
+    `streams` such clips at once from pinned host memory to pinned host
+    memory (saturated). The batch (one persistent launch for many frames)
+    takes spatial frames only, so it does not run this chain. And the fused
+    output's error against the FP64 oracle on a 256x128 window in the
+    middle of a frame with a history (the oracle fed the state the GPU
+    left: the crop of frame 1's mosaic developed from frame 0's state)."""
+    import torch
+    import libcraw_gb300 as L
+    from libcraw_gb300 import workloads as W
+
+    c = W.workload("serve_rcd_ap0")
+    w, h = c.width, c.height
+    prof = W.make_profile()
+    model = W.noise_model(c.noise_a_dn, c.noise_b_dn)
+    fp = L.frame_params(prof, denoise_strength=1.0, denoise_temporal_strength=0.8, noise_override=model,
+                        out_space=L.CS_ACES_AP1, out_space_set=1)
+    flags = L.FLAG_DENOISE | L.FLAG_TEMPORAL_DENOISE
+    movers = [(2.0, 0.5), (8.0, 2.0), (24.0, 10.0)]
+    host = [W.synth_frame(w, h, 60060 + i, frame=i, rects=256, zone_plates=4, noise_a_dn=c.noise_a_dn,
+                          noise_b_dn=c.noise_b_dn, movers=movers) for i in range(4)]
+    dev = [torch.from_numpy(f.view(np.int16)).cuda() for f in host]
+    srcs = [L.Image(t.data_ptr(), w * 2, L.FORMAT_R16_UNORM, w, h) for t in dev]
+    out = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    dst = L.Image(out.data_ptr(), w * 16, L.FORMAT_RGBA32F, w, h)
+    sptr = stream.cuda_stream
+    res = {"chain": f"{w}x{h} temporal 0.8 + NLM 1.0 + RCD + ACES AP1 (RGC) float32"}
+
+    def seq(impl, storage, n, keep=False):
+        pp = L.pipeline_params(w, h, debayer=L.DEBAYER_RCD, out_space=L.CS_ACES_AP1,
+                               flags=flags | (L.FLAG_KEEP_INTERMEDIATE if keep else 0),
+                               out_format=L.FORMAT_RGBA32F, storage=storage, impl=impl)
+        with L.Pipeline(ctx, pp) as pipe, torch.cuda.stream(stream):
+            for i in range(2):
+                pipe.record(sptr, srcs[i % 4], dst, fp)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            for i in range(n):
+                pipe.record(sptr, srcs[i % 4], dst, fp)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            return 1000.0 * n / e0.elapsed_time(e1)
+
+    res["plain_fp32_fps"] = seq(L.IMPL_PLAIN, L.STORAGE_FP32, plain_frames)
+    res["fused_fp16_fps"] = seq(L.IMPL_FUSED, L.STORAGE_FP16, nframes)
+    res["fused_fp32_fps"] = seq(L.IMPL_FUSED, L.STORAGE_FP32, nframes)
+
+    # Served: `streams` clips at once, every frame submitted up front.
+    pin_in = [torch.from_numpy(f.view(np.int16)).pin_memory() for f in host]
+    outs = [torch.empty((h, w, 4), dtype=torch.float32).pin_memory() for _ in range(2 * streams)]
+    pp16 = L.pipeline_params(w, h, debayer=L.DEBAYER_RCD, out_space=L.CS_ACES_AP1, flags=flags,
+                             out_format=L.FORMAT_RGBA32F, storage=L.STORAGE_FP16)
+    with L.Server(ctx, L.server_params(hbm_budget=60 << 30, max_inflight=2 * streams,
+                                       slots_per_stream=2)) as srv:
+        sids = [srv.open(L.server_stream_params(pp16)) for _ in range(streams)]
+        t0 = time.perf_counter()
+        for i in range(nframes):
+            for k, sid in enumerate(sids):
+                o = outs[(i % 2) * streams + k]
+                srv.submit(sid, pin_in[(i + k) % 4].data_ptr(), w * 2, o.data_ptr(), w * 16, fp, i / 24.0,
+                           (k << 32) | i)
+        srv.drain()
+        wall = time.perf_counter() - t0
+        got = []
+        while True:
+            r = srv.poll(256, 0)
+            if not r:
+                break
+            got += r
+    res["served_fp16"] = {"streams": streams, "frames": len(got), "fps": len(got) / wall,
+                          "device_ms_mean": float(np.mean([r.device_ms for r in got])),
+                          "how": "host to host: pinned mosaic in, pinned RGBA32F out, inside the timing"}
+    base = res["plain_fp32_fps"]
+    res["fused_fp16_vs_plain_fp32"] = res["fused_fp16_fps"] / base
+    res["served_fp16_vs_plain_fp32"] = res["served_fp16"]["fps"] / base
+    res["batch"] = "not run: the persistent batch launch carries spatial frames only"
+
+    # The error against FP64 on a central window of frame 1 (history from frame 0).
+    sys.path.insert(0, str(ROOT / "tests"))
+    from gpu_util import download_image
+    from oracle import Oracle, max_rel, psnr
+    orc = Oracle()
+    pp = L.pipeline_params(w, h, debayer=L.DEBAYER_RCD, out_space=L.CS_ACES_AP1,
+                           flags=flags | L.FLAG_KEEP_INTERMEDIATE, out_format=L.FORMAT_RGBA32F,
+                           storage=L.STORAGE_FP16)
+    x, y, ww, hh, mg = 2816, 1568, 256, 128, 32
+    x0, y0, x1, y1 = x - mg, y - mg, x + ww + mg, y + hh + mg
+    with L.Pipeline(ctx, pp) as pipe, torch.cuda.stream(stream):
+        pipe.record(sptr, srcs[0], dst, fp)
+        torch.cuda.synchronize()
+        lvl, var = pipe.temporal_state()
+        prev = np.stack([download_image(lvl, "r32f")[y0:y1, x0:x1].astype(np.float64),
+                         (download_image(var, "r8")[y0:y1, x0:x1].astype(np.float64) / 255.0) ** 2])
+        pipe.record(sptr, srcs[1], dst, fp)
+        torch.cuda.synchronize()
+        got = out[y:y + hh, x:x + ww].cpu().numpy()
+    crop = np.ascontiguousarray(host[1][y0:y1, x0:x1])
+    mos64, _ = orc.denoise_temporal(crop, prof, model, 1.0, 0.8, prev=np.ascontiguousarray(prev), s="f64")
+    pp0 = L.pipeline_params(x1 - x0, y1 - y0, debayer=L.DEBAYER_RCD, out_space=L.CS_ACES_AP1,
+                            out_format=L.FORMAT_RGBA32F)
+    fp0 = L.frame_params(prof, out_space=L.CS_ACES_AP1, out_space_set=1)
+    ref = orc.process(mos64, pp0, fp0, "f64")[mg:mg + hh, mg:mg + ww]
+    res["fused_fp16_vs_fp64_window"] = {"max_rel": max_rel(got, ref), "psnr_db": psnr(got, ref),
+                                        "window": [x, y, ww, hh]}
     return res
 
 

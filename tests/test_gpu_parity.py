@@ -66,6 +66,33 @@ def test_develop_vs_oracle(ctx, deb, cs, storage):
         assert max_rel(got, orc.process(m, pp, fp, "f64")) < 1e-3
 
 
+@pytest.mark.parametrize("storage", [L.STORAGE_FP32, L.STORAGE_FP16])
+def test_config1_at_its_size(ctx, storage):
+    """The plain-method configuration at its stated size and noise: one
+    1920x1080 frame (12-bit, black 256, white 4095, 64 rectangles and a zone
+    plate, var = 2 s + 16 DN^2), bilinear debayer, no denoise, BT.709 linear
+    float32, AWB histogram. FP32 storage within 2e-4 of the float oracle and
+    1e-3 of the double one (the reference's debayer checks,
+    tests/test_pipeline.c:6019-6111, hold their GPU output to the same
+    kind of bound); FP16 storage (the debayered values rounded to half)
+    within 2e-3 of both."""
+    c = W.workload("bilinear_bt709_1080p")
+    assert (c.width, c.height, c.noise_a_dn, c.noise_b_dn) == (1920, 1080, 2.0, 16.0)
+    assert c.debayer == L.DEBAYER_BILINEAR and c.out_space == L.CS_BT709
+    m = c.frame()
+    prof = W.make_profile()
+    pp = L.pipeline_params(c.width, c.height, debayer=c.debayer, out_space=c.out_space, flags=c.flags,
+                           out_format=L.FORMAT_RGBA32F, storage=storage)
+    fp = L.frame_params(prof)
+    got = run(ctx, m, pp, fp)
+    assert not np.isnan(got).any() and np.all(got[..., 3] == 1.0)
+    r32, r64 = max_rel(got, orc.process(m, pp, fp, "f32")), max_rel(got, orc.process(m, pp, fp, "f64"))
+    if storage == L.STORAGE_FP32:
+        assert r32 < 2e-4 and r64 < 1e-3, (r32, r64)
+    else:
+        assert r32 < TOL_FP16 and r64 < TOL_FP16, (r32, r64)
+
+
 @pytest.mark.parametrize("impl", [L.IMPL_FUSED, L.IMPL_PLAIN])
 def test_full_chain_vs_oracle(ctx, impl):
     """The single-frame chain of the headline workload at a small size:
