@@ -54,10 +54,15 @@ static const char *const plain_stage_names[ST_NB] = {
     "denoise_round",
 };
 
-/* One host-visible AWB slot: the three histograms, then the deferred
- * blocks and their count, all pinned so one async copy fills them. */
+/* One AWB slot. On the host, pinned: the three histograms, the count of
+ * deferred blocks and the first CRAW_K_AWB_DEFER_MAX of them, filled by
+ * two async copies. On the device: the slot's whole list of deferred
+ * blocks (its count, then one entry per 8x8 block of the frame at most),
+ * from which a count above CRAW_K_AWB_DEFER_MAX is read on demand. */
+#define SLOT_BYTES (HIST_BYTES + 16 + DEFER_BYTES)
 struct awb_slot {
-    uint8_t *host;            /* HIST_BYTES + DEFER_BYTES + 4 */
+    uint8_t *host;            /* SLOT_BYTES */
+    uint8_t *list;            /* device: 16 + nb_blocks * sizeof(CRAWKAwbDeferred) */
     bool folded;              /* deferred blocks already binned */
 };
 
@@ -87,7 +92,7 @@ struct CRAWPipeline {
     void *q, *qf;     size_t q_pitch;
     int qw, qh;
     uint64_t *awb_rec;
-    uint8_t *awb_dev;         /* HIST_BYTES + DEFER_BYTES + 4, mirrors a slot */
+    uint8_t *awb_dev;         /* HIST_BYTES: the histograms being built */
     uint32_t nb_blocks;
     uint32_t *kerr;           /* CRAW_K_ERR_* bits the kernels set */
     uint32_t *round_flags;    /* marks of the exact rounding, CRAW_K_ROUND_WORDS */
@@ -149,9 +154,11 @@ static void release(CRAWPipeline *p)
     for (size_t i = 0; i < CRAW_ARRAY_ELEMS(bufs); i++)
         craw_dev_free(ctx, bufs[i]);
     craw_dev_sync(ctx);
-    for (uint32_t i = 0; i < 4; i++)
+    for (uint32_t i = 0; i < 4; i++) {
+        craw_dev_free(ctx, p->slots[i].list);
         if (p->slots[i].host)
             cudaFreeHost(p->slots[i].host);
+    }
     for (int s = 0; s < CRAW_PIPELINE_PROFILE_SLOTS; s++)
         for (int i = 0; i < MAX_STAGES; i++)
             for (int j = 0; j < 2; j++)
@@ -482,15 +489,17 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
     if (p->awb) {
         p->nb_blocks = ((w + 7) / 8) * ((h + 7) / 8);
         if ((ret = craw_dev_alloc(ctx, (void **)&p->awb_rec, (size_t)p->nb_blocks * 8)) < 0 ||
-            (ret = craw_dev_alloc(ctx, (void **)&p->awb_dev, HIST_BYTES + DEFER_BYTES + 16)) < 0)
+            (ret = craw_dev_alloc(ctx, (void **)&p->awb_dev, HIST_BYTES)) < 0)
             goto fail;
         for (uint32_t i = 0; i < p->nb_slots; i++) {
-            if (cudaHostAlloc((void **)&p->slots[i].host, HIST_BYTES + DEFER_BYTES + 16,
-                              cudaHostAllocDefault) != cudaSuccess) {
+            if ((ret = craw_dev_alloc(ctx, (void **)&p->slots[i].list,
+                                      16 + (size_t)p->nb_blocks * sizeof(CRAWKAwbDeferred))) < 0)
+                goto fail;
+            if (cudaHostAlloc((void **)&p->slots[i].host, SLOT_BYTES, cudaHostAllocDefault) != cudaSuccess) {
                 ret = CRAW_ERROR(ENOMEM);
                 goto fail;
             }
-            memset(p->slots[i].host, 0, HIST_BYTES + DEFER_BYTES + 16);
+            memset(p->slots[i].host, 0, SLOT_BYTES);
         }
     }
     if ((ret = craw_dev_alloc(ctx, (void **)&p->kerr, 16)) < 0)
@@ -671,10 +680,11 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
     uint8_t *awb_hist = NULL;
     CRAWKAwbOut awb = { 0 };
     if (p->awb) {
+        uint8_t *list = p->slots[p->nb_recorded % p->nb_slots].list;
         awb_hist = p->awb_dev;
         awb.rec = p->plain ? NULL : p->awb_rec;
-        awb.deferred = (CRAWKAwbDeferred *)(p->awb_dev + HIST_BYTES);
-        awb.nb_deferred = (uint32_t *)(p->awb_dev + HIST_BYTES + DEFER_BYTES);
+        awb.deferred = (CRAWKAwbDeferred *)(list + 16);
+        awb.nb_deferred = (uint32_t *)list;
         if (cudaMemsetAsync(awb_hist, 0, HIST_BYTES, s) != cudaSuccess ||
             cudaMemsetAsync(awb.nb_deferred, 0, 4, s) != cudaSuccess)
             return CRAW_ERROR(EIO);
@@ -820,8 +830,9 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
             if (ret < 0)
                 goto launch_fail;
         }
-        if (cudaMemcpyAsync(slot->host, p->awb_dev, HIST_BYTES + DEFER_BYTES + 4,
-                            cudaMemcpyDeviceToHost, s) != cudaSuccess) {
+        if (cudaMemcpyAsync(slot->host, p->awb_dev, HIST_BYTES, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaMemcpyAsync(slot->host + HIST_BYTES, slot->list, 16 + DEFER_BYTES, cudaMemcpyDeviceToHost,
+                            s) != cudaSuccess) {
             ret = CRAW_ERROR(EIO);
             goto launch_fail;
         }
@@ -868,16 +879,29 @@ CRAW_API int craw_pipeline_get_awb_histogram_n(CRAWPipeline *p, uint32_t frames_
     slot = &p->slots[(p->nb_recorded - 1 - frames_back) % p->nb_slots];
     hist = (uint32_t *)slot->host;
     if (!slot->folded) {
-        /* Bin the blocks the device deferred, with this host's logf. */
-        const CRAWKAwbDeferred *d = (const CRAWKAwbDeferred *)(slot->host + HIST_BYTES);
-        uint32_t nd = *(const uint32_t *)(slot->host + HIST_BYTES + DEFER_BYTES);
-        if (nd > CRAW_K_AWB_DEFER_MAX) {
-            craw_log(p->ctx, CRAW_LOG_WARN, "%u AWB blocks sat on bin edges; %u were binned on "
-                     "the device\n", nd, nd - CRAW_K_AWB_DEFER_MAX);
-            nd = CRAW_K_AWB_DEFER_MAX;
-        }
-        for (uint32_t i = 0; i < nd; i++)
+        /* Bin the blocks the device deferred, with this host's logf: the
+         * first CRAW_K_AWB_DEFER_MAX came with the slot, the rest (a frame
+         * with that many blocks on bin edges) are read from the slot's
+         * device list now. */
+        const CRAWKAwbDeferred *d = (const CRAWKAwbDeferred *)(slot->host + HIST_BYTES + 16);
+        const uint32_t nd = *(const uint32_t *)(slot->host + HIST_BYTES);
+        const uint32_t nd0 = CRAW_MIN(nd, (uint32_t)CRAW_K_AWB_DEFER_MAX);
+        for (uint32_t i = 0; i < nd0; i++)
             craw_awb_bin_host(d[i].rr, d[i].bb, d[i].g, hist, hist + HIST_N, hist + 2 * HIST_N);
+        if (nd > nd0) {
+            CRAWKAwbDeferred *rest = malloc((size_t)(nd - nd0) * sizeof(*rest));
+            if (!rest)
+                return CRAW_ERROR(ENOMEM);
+            cudaSetDevice(p->ctx->device);
+            if (cudaMemcpy(rest, slot->list + 16 + (size_t)nd0 * sizeof(*rest), (size_t)(nd - nd0) * sizeof(*rest),
+                           cudaMemcpyDeviceToHost) != cudaSuccess) {
+                free(rest);
+                return CRAW_ERROR(EIO);
+            }
+            for (uint32_t i = 0; i < nd - nd0; i++)
+                craw_awb_bin_host(rest[i].rr, rest[i].bb, rest[i].g, hist, hist + HIST_N, hist + 2 * HIST_N);
+            free(rest);
+        }
         slot->folded = true;
     }
     out->bins = CRAW_AWB_HIST_BINS;

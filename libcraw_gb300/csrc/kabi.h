@@ -162,7 +162,9 @@ typedef struct CRAWKDevelop {
  * min(g, 0.5), 30-45 the 16.16 weight g^4. Blocks whose bin is within
  * rounding of a bin edge are not binned on the device: their raw ratios go
  * to the deferred list and the host bins them with its own logf, so the
- * histogram is bit for bit the CPU builder's. */
+ * histogram is bit for bit the CPU builder's. The host copy of a slot
+ * holds the first CRAW_K_AWB_DEFER_MAX; more are read from the device
+ * list when the histogram is asked for. */
 #define CRAW_K_AWB_VALID (1ull << 46)
 #define CRAW_K_AWB_DEFER_MAX 4096
 
@@ -173,7 +175,7 @@ typedef struct CRAWKAwbDeferred {
 
 typedef struct CRAWKAwbOut {
     uint64_t *rec;                 /* ceil(w/8) * ceil(h/8) records, or NULL */
-    CRAWKAwbDeferred *deferred;    /* CRAW_K_AWB_DEFER_MAX entries */
+    CRAWKAwbDeferred *deferred;    /* room for one entry per 8x8 block of the frame */
     uint32_t *nb_deferred;         /* counter, zeroed before the frame */
 } CRAWKAwbOut;
 

@@ -161,7 +161,7 @@ k_chroma_up_color(const CRAWKDevelop k, const CRAWKChroma c, const void *inter, 
         float n = (float)(xe * ye);
         awb.rec[(size_t)(y0 / 8 + by) * blocks_x + x0 / 8 + bx] =
             craw_awb_block(__fdiv_rn(s0, n), __fdiv_rn(s1, n), __fdiv_rn(s2, n), k.awb_wb,
-                           awb.deferred, awb.nb_deferred);
+                           awb.deferred, awb.nb_deferred, craw_awb_blocks(k.width, k.height));
     }
 }
 

@@ -215,6 +215,12 @@ CRAW_DEV void craw_load_rgb(const void *base, size_t pitch, int x, int y, int ha
     }
 }
 
+/* The frame's 8x8 blocks: a deferred-block list this long never fills. */
+CRAW_DEV uint32_t craw_awb_blocks(int w, int h)
+{
+    return (uint32_t)((w + 7) / 8) * (uint32_t)((h + 7) / 8);
+}
+
 /* The AWB statistic of one block from its mean (reference
  * lib/awb.c:255-291, whose operation order is kept so that the bins and
  * weights are the CPU builder's bit for bit): skip clipped and near-black
@@ -229,7 +235,7 @@ CRAW_DEV void craw_load_rgb(const void *base, size_t pitch, int x, int y, int ha
  * of its FP32 rate, so a double-precision log would cost more than the
  * whole block sum.) */
 CRAW_DEV uint64_t craw_awb_block(float r, float g, float b, const float wb[3],
-                                 CRAWKAwbDeferred *deferred, uint32_t *nb_deferred)
+                                 CRAWKAwbDeferred *deferred, uint32_t *nb_deferred, uint32_t cap)
 {
     const float lmin = -2.5f, lmax = 1.0f, span = lmax - lmin;
     if (fmaxf(fmaxf(r, g), b) >= 0.98f || g < 0.002f)
@@ -247,7 +253,7 @@ CRAW_DEV uint64_t craw_awb_block(float r, float g, float b, const float wb[3],
     const bool near_y = ry >= 1.0f && ry <= 127.0f && fabsf(fy - ry) < 2e-4f;
     if (deferred && (near_x || near_y)) {
         uint32_t i = atomicAdd(nb_deferred, 1u);
-        if (i < CRAW_K_AWB_DEFER_MAX) {
+        if (i < cap) {
             CRAWKAwbDeferred d;
             d.rr = rr; d.bb = bb; d.g = g; d.pad = 0;
             deferred[i] = d;

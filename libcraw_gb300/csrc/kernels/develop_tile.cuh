@@ -669,7 +669,8 @@ CRAW_DEV void awb_blocks(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0
         float n = (float)(xe * ye);
         io.awb.rec[(size_t)(y0 / 8 + by) * blocks_x + x0 / 8 + bx] =
             craw_awb_block(__fdiv_rn(s0, n), __fdiv_rn(s1, n), __fdiv_rn(s2, n), k.awb_wb,
-                           io.awb.deferred, io.awb.nb_deferred);
+                           io.awb.deferred, io.awb.nb_deferred,
+                           craw_awb_blocks(k.width, k.height));
     }
 }
 

@@ -414,7 +414,7 @@ __global__ void p_awb(const CRAWKDevelop k, const float *inter, size_t ip, uint3
     }
     float n = (float)(xe * ye);
     uint64_t r = craw_awb_block(__fdiv_rn(s0, n), __fdiv_rn(s1, n), __fdiv_rn(s2, n), k.awb_wb,
-                                awb.deferred, awb.nb_deferred);
+                                awb.deferred, awb.nb_deferred, craw_awb_blocks(k.width, k.height));
     if (r & CRAW_K_AWB_VALID) {
         uint32_t bin = (uint32_t)(r & 0x3fffu);
         atomicAdd(&hist[bin], 1u);

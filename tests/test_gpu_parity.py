@@ -227,6 +227,48 @@ def test_awb_bit_exact(ctx, deb, storage, chroma):
     assert np.array_equal(ocnt, cnt)
 
 
+def test_awb_many_edge_blocks(ctx):
+    """More blocks on AWB bin edges than a slot carries to the host (4096):
+    flat 64x64 regions of two colours whose R/G ratio puts ln(R/G) on a bin
+    edge to within 1e-6 of a bin, 1024x1024 pixels (16384 blocks). The
+    device defers every such block; the histogram is still the CPU
+    builder's on the GPU's intermediate, bit for bit (the blocks past the
+    slot's 4096 are read from its device list)."""
+    from gpu_util import download_image, upload_mosaic, alloc_rgba
+    w = h = 1024
+    codes = [(519, 1029, 700), (1073, 977, 1300)]   # (R, G, B) raw codes
+    m = np.empty((h, w), np.uint16)
+    for ry in range(0, h, 64):
+        for rx in range(0, w, 64):
+            r, g, b = codes[((rx // 64) + (ry // 64)) & 1]
+            blk = m[ry:ry + 64, rx:rx + 64]
+            blk[0::2, 0::2] = r
+            blk[0::2, 1::2] = g
+            blk[1::2, 0::2] = g
+            blk[1::2, 1::2] = b
+    prof = W.make_profile()
+    pp = L.pipeline_params(w, h, flags=L.FLAG_AWB_HISTOGRAM | L.FLAG_KEEP_INTERMEDIATE, out_format=L.FORMAT_RGBA32F)
+    fp = L.frame_params(prof)
+    with L.Pipeline(ctx, pp) as pipe:
+        _, src = upload_mosaic(m)
+        _, dst = alloc_rgba(w, h)
+        pipe.record(torch.cuda.current_stream().cuda_stream, src, dst, fp)
+        torch.cuda.synchronize()
+        rgb_img, _ = pipe.intermediate()
+        rgb = download_image(rgb_img, "rgba32f").astype(np.float32)
+        hist = pipe.awb_histogram()
+    # How many blocks lie within the device's deferral margin of a bin edge.
+    means = rgb[..., :3].reshape(h // 8, 8, w // 8, 8, 3).astype(np.float64).mean(axis=(1, 3))
+    with np.errstate(divide="ignore", invalid="ignore"):
+        fx = (np.log(means[..., 0] / W.WB[0] / means[..., 1]) + 2.5) / 3.5 * 128
+    near = np.abs(fx - np.rint(fx)) < 2e-4
+    assert near.sum() > 4096, near.sum()
+    cnt, wgt, brt = L.awb_histogram_from_rgb(rgb, W.WB)
+    assert np.array_equal(hist.count, cnt)
+    assert np.array_equal(hist.weight, wgt)
+    assert np.array_equal(hist.weight_bright, brt)
+
+
 def test_chroma_vs_oracle(ctx):
     w, h = 240, 160
     c = W.workload("temporal_mhc_p3", w, h)
