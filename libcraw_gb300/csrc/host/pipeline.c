@@ -62,7 +62,8 @@ static const char *const plain_stage_names[ST_NB] = {
 #define SLOT_BYTES (HIST_BYTES + 16 + DEFER_BYTES)
 struct awb_slot {
     uint8_t *host;            /* SLOT_BYTES */
-    uint8_t *list;            /* device: 16 + nb_blocks * sizeof(CRAWKAwbDeferred) */
+    uint8_t *list;            /* device: the count (16 B), then room for
+                               * max(nb_blocks, CRAW_K_AWB_DEFER_MAX) entries */
     bool folded;              /* deferred blocks already binned */
 };
 
@@ -492,8 +493,11 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
             (ret = craw_dev_alloc(ctx, (void **)&p->awb_dev, HIST_BYTES)) < 0)
             goto fail;
         for (uint32_t i = 0; i < p->nb_slots; i++) {
+            /* Room for every block, and at least for the part the slot's
+             * async copy reads. */
+            const size_t entries = CRAW_MAX((size_t)p->nb_blocks, (size_t)CRAW_K_AWB_DEFER_MAX);
             if ((ret = craw_dev_alloc(ctx, (void **)&p->slots[i].list,
-                                      16 + (size_t)p->nb_blocks * sizeof(CRAWKAwbDeferred))) < 0)
+                                      16 + entries * sizeof(CRAWKAwbDeferred))) < 0)
                 goto fail;
             if (cudaHostAlloc((void **)&p->slots[i].host, SLOT_BYTES, cudaHostAllocDefault) != cudaSuccess) {
                 ret = CRAW_ERROR(ENOMEM);
