@@ -23,6 +23,7 @@ craw_profile_eval / colorspace ...    module functions of the same names
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 import errno as _errno
 import os
 from pathlib import Path
@@ -571,6 +572,7 @@ class Context:
         params = CudaInitParams(device, None)
         opts = ContextOptions()
         opts.log_level = 2 if log_level is None else log_level
+        self._children = weakref.WeakSet()
         _check(lib().craw_context_create(C.byref(self._h), C.byref(params), C.byref(opts)),
                "craw_context_create")
         self.device = device
@@ -580,6 +582,12 @@ class Context:
         return self._h
 
     def close(self) -> None:
+        """Frees the context, and first every pipeline, server and batch
+        still open on it (they hold its device memory and stream; the
+        garbage collector may finalise a context before objects that refer
+        to it when they sit in one reference cycle)."""
+        for child in list(getattr(self, "_children", ())):
+            child.close()
         if self._h:
             lib().craw_context_free(C.byref(self._h))
 
@@ -608,6 +616,7 @@ class Pipeline:
         self.ctx = ctx
         self.params = params
         self._h = C.c_void_p()
+        ctx._children.add(self)
         _check(lib().craw_pipeline_create(ctx.handle, C.byref(params), C.byref(self._h)),
                "craw_pipeline_create")
 
@@ -766,6 +775,7 @@ class Server:
     def __init__(self, ctx: Context, params: ServerParams):
         self.ctx = ctx
         self._h = C.c_void_p()
+        ctx._children.add(self)
         _check(lib().craw_server_create(ctx.handle, C.byref(params), C.byref(self._h)),
                "craw_server_create")
 
@@ -830,6 +840,7 @@ class Batch:
         self.ctx = ctx
         self.params = params
         self._h = C.c_void_p()
+        ctx._children.add(self)
         _check(lib().craw_batch_create(ctx.handle, C.byref(params), C.byref(self._h)),
                "craw_batch_create")
 

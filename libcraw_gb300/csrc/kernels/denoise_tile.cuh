@@ -232,8 +232,11 @@ struct Search {
                     }
                     wsum[m][j] += wa;
                     wsum[m + 1][j] += wb;
-                    acc[m][j] = fmaf(wa, win[m + 1][j + 1 + dx + S], acc[m][j]);
-                    acc[m + 1][j] = fmaf(wb, win[m + 2][j + 1 + dx + S], acc[m + 1][j]);
+                    /* Centred on the sample's own value, so that the sum's
+                     * rounding scales with the spread of the values around
+                     * it rather than with their level. */
+                    acc[m][j] = fmaf(wa, win[m + 1][j + 1 + dx + S] - own[m + 1][j + 1], acc[m][j]);
+                    acc[m + 1][j] = fmaf(wb, win[m + 2][j + 1 + dx + S] - own[m + 2][j + 1], acc[m + 1][j]);
                 }
             }
         }
@@ -256,6 +259,12 @@ struct SearchX2 {
     f2x acc[M], wsum[M];
     f2x nkl[HISTORY ? M : 1], lvc[HISTORY ? M : 1];
     f2x c1, c0;
+
+    /* The two samples' own values in patch-block row r: columns 1 and 2. */
+    CRAW_DEV f2x own_c(int r) const
+    {
+        return f2_pack(f2_hi(own[r][0]), f2_lo(own[r][1]));
+    }
 
     CRAW_DEV void init(const float *To, const float *Vp, int ox0, int oy0, float inv_h2)
     {
@@ -339,8 +348,9 @@ struct SearchX2 {
                 const f2x qb = (o & 1) ? ev[m + 2][(o + 1) >> 1] : od[m + 2][o >> 1];
                 wsum[m] = f2_add(wsum[m], wa);
                 wsum[m + 1] = f2_add(wsum[m + 1], wb);
-                acc[m] = f2_fma(wa, qa, acc[m]);
-                acc[m + 1] = f2_fma(wb, qb, acc[m + 1]);
+                /* Centred on the samples' own values (Search). */
+                acc[m] = f2_fma(wa, f2_sub(qa, own_c(m + 1)), acc[m]);
+                acc[m + 1] = f2_fma(wb, f2_sub(qb, own_c(m + 2)), acc[m + 1]);
             }
         }
     }
@@ -479,8 +489,9 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
             st.step_dy(Tp, To, Vp, Vo, ox0, oy0, dy);
 #pragma unroll
         for (int m = 0; m < M; m++) {
-            res[m][0] = __fdiv_rn(f2_lo(st.acc[m]), f2_lo(st.wsum[m]));
-            res[m][1] = __fdiv_rn(f2_hi(st.acc[m]), f2_hi(st.wsum[m]));
+            const f2x c = st.own_c(m + 1);
+            res[m][0] = f2_lo(c) + __fdiv_rn(f2_lo(st.acc[m]), f2_lo(st.wsum[m]));
+            res[m][1] = f2_hi(c) + __fdiv_rn(f2_hi(st.acc[m]), f2_hi(st.wsum[m]));
         }
     } else if constexpr (SPATIAL) {
         const float *Vp = V + pl * C::TN;
@@ -495,7 +506,7 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
         for (int m = 0; m < M; m++)
 #pragma unroll
             for (int j = 0; j < BW; j++)
-                res[m][j] = __fdiv_rn(st.acc[m][j], st.wsum[m][j]);
+                res[m][j] = st.own[m + 1][j + 1] + __fdiv_rn(st.acc[m][j], st.wsum[m][j]);
     }
 
     /* ---- outputs: the next state, and the denoised mosaic in its raw

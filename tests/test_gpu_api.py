@@ -232,3 +232,22 @@ def test_awb_requires_flag(ctx):
         with pytest.raises(L.CrawError) as e:
             pipe.awb_histogram()
         assert e.value.errno == 22
+
+
+def test_context_closes_its_pipelines_first():
+    """Closing a context frees the pipelines still open on it first, so
+    that a later close (or the garbage collector finalising the two in
+    either order) never touches freed memory."""
+    import gc
+    c = L.Context(0)
+    p = L.Pipeline(c, L.pipeline_params(64, 48, flags=L.FLAG_DENOISE))
+    c.close()
+    assert not p._h
+    p.close()
+    # A reference cycle holding both: collected in whatever order.
+    c2 = L.Context(0)
+    p2 = L.Pipeline(c2, L.pipeline_params(64, 48))
+    cyc = [c2, p2]
+    cyc.append(cyc)
+    del c2, p2, cyc
+    gc.collect()
