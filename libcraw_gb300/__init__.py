@@ -23,7 +23,6 @@ craw_profile_eval / colorspace ...    module functions of the same names
 from __future__ import annotations
 
 import ctypes as C
-import weakref
 import errno as _errno
 import os
 from pathlib import Path
@@ -572,7 +571,7 @@ class Context:
         params = CudaInitParams(device, None)
         opts = ContextOptions()
         opts.log_level = 2 if log_level is None else log_level
-        self._children = weakref.WeakSet()
+        self._children = []
         _check(lib().craw_context_create(C.byref(self._h), C.byref(params), C.byref(opts)),
                "craw_context_create")
         self.device = device
@@ -581,13 +580,23 @@ class Context:
     def handle(self):
         return self._h
 
+    def _own(self, handle: C.c_void_p, free: str) -> None:
+        """Records the handle box of a pipeline, server or batch created on
+        this context and the name of its free function. The box itself is
+        kept (not the Python object): the garbage collector clears weak
+        references before it finalises a reference cycle, and may finalise
+        the context before the objects that refer to it."""
+        self._children = [(h, f) for h, f in self._children if h] + [(handle, free)]
+
     def close(self) -> None:
         """Frees the context, and first every pipeline, server and batch
-        still open on it (they hold its device memory and stream; the
-        garbage collector may finalise a context before objects that refer
-        to it when they sit in one reference cycle)."""
-        for child in list(getattr(self, "_children", ())):
-            child.close()
+        still open on it (they hold its device memory and stream). Each
+        shares its handle box with its object, so the object's own close
+        then finds it freed."""
+        for h, free in reversed(getattr(self, "_children", ())):
+            if h:
+                getattr(lib(), free)(C.byref(h))
+        self._children = []
         if self._h:
             lib().craw_context_free(C.byref(self._h))
 
@@ -616,7 +625,7 @@ class Pipeline:
         self.ctx = ctx
         self.params = params
         self._h = C.c_void_p()
-        ctx._children.add(self)
+        ctx._own(self._h, "craw_pipeline_free")
         _check(lib().craw_pipeline_create(ctx.handle, C.byref(params), C.byref(self._h)),
                "craw_pipeline_create")
 
@@ -775,7 +784,7 @@ class Server:
     def __init__(self, ctx: Context, params: ServerParams):
         self.ctx = ctx
         self._h = C.c_void_p()
-        ctx._children.add(self)
+        ctx._own(self._h, "craw_server_free")
         _check(lib().craw_server_create(ctx.handle, C.byref(params), C.byref(self._h)),
                "craw_server_create")
 
@@ -840,7 +849,7 @@ class Batch:
         self.ctx = ctx
         self.params = params
         self._h = C.c_void_p()
-        ctx._children.add(self)
+        ctx._own(self._h, "craw_batch_free")
         _check(lib().craw_batch_create(ctx.handle, C.byref(params), C.byref(self._h)),
                "craw_batch_create")
 
