@@ -11,19 +11,20 @@ namespace {
 
 using namespace craw_dn;
 
-template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2>
+/* MARK: the exact rounding's marks (spatial denoise only). */
+template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2, bool MARK>
 __global__ void __launch_bounds__(Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY>::NT)
 k_denoise(const CRAWKDenoise k, const CRAWKDenoiseIO io, const CRAWKRound rd)
 {
     extern __shared__ __align__(16) float smem[];
-    denoise_tile<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2>(k, io, blockIdx.x, blockIdx.y, smem, &rd);
+    denoise_tile<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2, true, MARK>(k, io, blockIdx.x, blockIdx.y, smem, &rd);
 }
 
-template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2>
+template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2, bool MARK = false>
 int launch(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, const CRAWKRound *rd, cudaStream_t s)
 {
     using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2>;
-    auto fn = k_denoise<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2>;
+    auto fn = k_denoise<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2, MARK>;
     const size_t smem = (size_t)C::smem_floats * sizeof(float);
     static std::atomic<uint64_t> attr_done{ 0 };
     if (craw_smem_attr(fn, smem, attr_done) < 0)
@@ -40,6 +41,8 @@ int dispatch(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, const CRAWKRound *
 {
     const bool sp = k->mode & CRAW_K_DN_SPATIAL, te = k->mode & CRAW_K_DN_TEMPORAL;
     const bool hi = te && (k->mode & CRAW_K_DN_HISTORY);
+    if (sp && !te && rd && rd->flags)
+        return launch<BW, M, WP, true, false, false, X2, true>(k, io, rd, s);
     if (sp && !te)  return launch<BW, M, WP, true, false, false, X2>(k, io, rd, s);
     if (sp && !hi)  return launch<BW, M, WP, true, true, false, X2>(k, io, rd, s);
     if (sp)         return launch<BW, M, WP, true, true, true, X2>(k, io, rd, s);

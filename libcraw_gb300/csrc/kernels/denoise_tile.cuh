@@ -130,7 +130,7 @@ struct Cfg {
  * expanded as 2^min(log2(e) + vq * lvc + d2 * nkl, 0) with the centre's
  * lvc = log2(e)/vc and nkl = -lvc/(9h^2) taken out of the search: two
  * multiply-adds an offset. */
-template <int BW, int M, int R, int TS, bool HISTORY>
+template <int BW, int M, int R, int TS, bool HISTORY, bool CENTRE>
 struct Search {
     static_assert(BW % 2 == 0 && M % 2 == 0, "pairs of columns and rows");
     float own[M + 2][BW + 2];
@@ -232,11 +232,16 @@ struct Search {
                     }
                     wsum[m][j] += wa;
                     wsum[m + 1][j] += wb;
-                    /* Centred on the sample's own value, so that the sum's
-                     * rounding scales with the spread of the values around
-                     * it rather than with their level. */
-                    acc[m][j] = fmaf(wa, win[m + 1][j + 1 + dx + S] - own[m + 1][j + 1], acc[m][j]);
-                    acc[m + 1][j] = fmaf(wb, win[m + 2][j + 1 + dx + S] - own[m + 2][j + 1], acc[m + 1][j]);
+                    if constexpr (CENTRE) {
+                        /* Centred on the sample's own value, so that the
+                         * sum's rounding scales with the spread of the
+                         * values around it rather than with their level. */
+                        acc[m][j] = fmaf(wa, win[m + 1][j + 1 + dx + S] - own[m + 1][j + 1], acc[m][j]);
+                        acc[m + 1][j] = fmaf(wb, win[m + 2][j + 1 + dx + S] - own[m + 2][j + 1], acc[m + 1][j]);
+                    } else {
+                        acc[m][j] = fmaf(wa, win[m + 1][j + 1 + dx + S], acc[m][j]);
+                        acc[m + 1][j] = fmaf(wb, win[m + 2][j + 1 + dx + S], acc[m + 1][j]);
+                    }
                 }
             }
         }
@@ -251,7 +256,7 @@ struct Search {
  * one sample; with a history `Vp` / `Vo` are the variance and its shifted
  * copy. Same arithmetic as Search (without fused multiply-adds in the
  * squared differences). */
-template <int M, int R, int TS, bool HISTORY>
+template <int M, int R, int TS, bool HISTORY, bool CENTRE>
 struct SearchX2 {
     static_assert(M % 2 == 0, "pairs of rows");
     static_assert(R - 1 == S, "window origin");
@@ -260,10 +265,14 @@ struct SearchX2 {
     f2x nkl[HISTORY ? M : 1], lvc[HISTORY ? M : 1];
     f2x c1, c0;
 
-    /* The two samples' own values in patch-block row r: columns 1 and 2. */
-    CRAW_DEV f2x own_c(int r) const
+    /* The centres of the two samples of patch-block row r (columns 1 and
+     * 2) with CENTRE: the aligned pair of columns 0 and 1, each sample's
+     * left neighbour. Any centre leaves the exact sum unchanged; a
+     * neighbour's value lies as close to the window's values as the
+     * sample's own, up to the noise, and needs no packing. */
+    CRAW_DEV f2x centre(int r) const
     {
-        return f2_pack(f2_hi(own[r][0]), f2_lo(own[r][1]));
+        return own[r][0];
     }
 
     CRAW_DEV void init(const float *To, const float *Vp, int ox0, int oy0, float inv_h2)
@@ -348,19 +357,26 @@ struct SearchX2 {
                 const f2x qb = (o & 1) ? ev[m + 2][(o + 1) >> 1] : od[m + 2][o >> 1];
                 wsum[m] = f2_add(wsum[m], wa);
                 wsum[m + 1] = f2_add(wsum[m + 1], wb);
-                /* Centred on the samples' own values (Search). */
-                acc[m] = f2_fma(wa, f2_sub(qa, own_c(m + 1)), acc[m]);
-                acc[m + 1] = f2_fma(wb, f2_sub(qb, own_c(m + 2)), acc[m + 1]);
+                if constexpr (CENTRE) {
+                    acc[m] = f2_fma(wa, f2_sub(qa, centre(m + 1)), acc[m]);
+                    acc[m + 1] = f2_fma(wb, f2_sub(qb, centre(m + 2)), acc[m + 1]);
+                } else {
+                    acc[m] = f2_fma(wa, qa, acc[m]);
+                    acc[m + 1] = f2_fma(wb, qb, acc[m + 1]);
+                }
             }
         }
     }
 };
 
 /* One tile (tile column bx, tile row by) of all four planes; the whole
- * CTA takes part. `smem` holds Cfg::smem_floats floats. `rd`: NULL, or
- * the marking of samples whose code lies near a rounding boundary
- * (CRAWKRound). */
-template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2 = false, bool STAGED = true>
+ * CTA takes part. `smem` holds Cfg::smem_floats floats. MARK (spatial
+ * only): `rd` is the marking of samples whose code lies near a rounding
+ * boundary (CRAWKRound), and the weighted sums are centred, which makes
+ * their float error about 3x smaller at a boundary and the marked band
+ * narrower, for about 6 % more time in the search. */
+template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2 = false, bool STAGED = true,
+          bool MARK = false>
 CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int bx, int by, float *smem,
                            const CRAWKRound *rd = nullptr)
 {
@@ -375,7 +391,8 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
 
     const int tx0 = bx * OX, ty0 = by * OY;
     const int tid = threadIdx.x;
-    if (rd && rd->count2 && bx == 0 && by == 0 && tid == 0) {
+    static_assert(!MARK || (SPATIAL && !TEMPORAL && BW == 2), "marks: spatial, a half-warp a word");
+    if (MARK && rd->count2 && bx == 0 && by == 0 && tid == 0) {
         rd->count2[0] = 0;      /* this frame's list of undecided samples starts empty */
         rd->count2[1] = 0;      /* and so does the rounding's work counter */
     }
@@ -482,20 +499,24 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
     if constexpr (C::PACKED) {
         const float *To = smem + C::TO_OFF + pl * C::TN;
         const float *Vp = V + pl * C::TN, *Vo = smem + C::VO_OFF + pl * C::TN;
-        SearchX2<M, R, TS, HISTORY> st;
+        SearchX2<M, R, TS, HISTORY, MARK> st;
         st.init(To, Vp, ox0, oy0, k.inv_h2);
 #pragma unroll 1
         for (int dy = -S; dy <= S; dy++)
             st.step_dy(Tp, To, Vp, Vo, ox0, oy0, dy);
 #pragma unroll
         for (int m = 0; m < M; m++) {
-            const f2x c = st.own_c(m + 1);
-            res[m][0] = f2_lo(c) + __fdiv_rn(f2_lo(st.acc[m]), f2_lo(st.wsum[m]));
-            res[m][1] = f2_hi(c) + __fdiv_rn(f2_hi(st.acc[m]), f2_hi(st.wsum[m]));
+            res[m][0] = __fdiv_rn(f2_lo(st.acc[m]), f2_lo(st.wsum[m]));
+            res[m][1] = __fdiv_rn(f2_hi(st.acc[m]), f2_hi(st.wsum[m]));
+            if constexpr (MARK) {
+                const f2x c = st.centre(m + 1);
+                res[m][0] += f2_lo(c);
+                res[m][1] += f2_hi(c);
+            }
         }
     } else if constexpr (SPATIAL) {
         const float *Vp = V + pl * C::TN;
-        Search<BW, M, R, TS, HISTORY> st;
+        Search<BW, M, R, TS, HISTORY, MARK> st;
         st.init(Tp, Vp, ox0, oy0, k.inv_h2);
         /* dy is a runtime loop and only the seven dx of one dy are
          * unrolled, so that the loop body stays in the instruction cache. */
@@ -506,7 +527,8 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
         for (int m = 0; m < M; m++)
 #pragma unroll
             for (int j = 0; j < BW; j++)
-                res[m][j] = st.own[m + 1][j + 1] + __fdiv_rn(st.acc[m][j], st.wsum[m][j]);
+                res[m][j] = MARK ? st.own[m + 1][j + 1] + __fdiv_rn(st.acc[m][j], st.wsum[m][j])
+                                 : __fdiv_rn(st.acc[m][j], st.wsum[m][j]);
     }
 
     /* ---- outputs: the next state, and the denoised mosaic in its raw
@@ -517,7 +539,7 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
      * arrays with the warp's plane would copy them to local memory). */
     const float blk = pick4(k.black, pl), irng = pick4(k.inv_range, pl), rng = pick4(k.range, pl);
     /* The marks need a half-warp's 16 lanes x BW columns to be one word. */
-    const bool mark = BW == 2 && rd && rd->flags;
+    const bool mark = MARK && rd->flags;
 #pragma unroll
     for (int m = 0; m < M; m++) {
         const int qy = ty0 + oy0 + m;
