@@ -223,10 +223,10 @@ void craw_denoise_round_band(const CRAWKDenoise *k, float scale, CRAWKRound *rd)
     /* The float path's error in codes, about B ulps of t carried through
      * dx/dt = 65535 range (a/2) t (the inverse transform), plus a few ulps
      * of x itself (x <= 65535 black + 65535 range a/4 t^2) and of t near
-     * the transform's linear branch. With the weighted sums centred on the
-     * sample's own value, B = 6 makes the band at scale 1 about twice the
-     * largest error seen in the float evaluation; `scale` multiplies the
-     * whole band. */
+     * the transform's linear branch. With the weighted sums centred (the
+     * marking kernel sums w (q - c), c a neighbour's value), B = 6 makes the
+     * band at scale 1 about twice the largest error seen in the float
+     * evaluation; `scale` multiplies the whole band (2 by default). */
     const double B = 6.0 * 0x1p-24, X = 2.0 * 0x1p-24;
     double rmax = 0.0, bmax = 0.0;
     for (int s = 0; s < 4; s++) {
