@@ -22,6 +22,12 @@ CRAW_API int craw_debug_force_denoise_shape(int shape);
  * comparing the two. Returns the previous setting. */
 CRAW_API int craw_debug_rcd_tma(int on);
 
+/* 1 (default): the denoise's interior tiles (packed kernels, spatial
+ * filtering) bring their mosaic region into shared memory with one TMA
+ * tile copy each; 0: with plain loads, for comparing the two. Returns the
+ * previous setting. */
+CRAW_API int craw_debug_denoise_tma(int on);
+
 struct CRAWPipeline;
 
 /* Waits for the pipeline's recordings to finish and returns the error

@@ -175,7 +175,7 @@ static int batch_autotune(CRAWBatch *b)
             float t = 0.0f, ms = 1e30f;
             for (int r = 0; r < 3; r++) {
                 cudaEventRecord(e0, ctx->stream);
-                if (craw_k_denoise(&F->dn, &F->dio, shape, NULL, ctx->stream) < 0) {
+                if (craw_k_denoise(&F->dn, &F->dio, shape, NULL, NULL, ctx->stream) < 0) {
                     ret = CRAW_ERROR(EIO);
                     goto done;
                 }
@@ -403,7 +403,8 @@ CRAW_API int craw_batch_record(CRAWBatch *b, cudaStream_t s, uint32_t nb, const 
     if (ns > 0 && (ret = batch_persistent(b, s, ns, w, h, dn)) < 0)
         return ret;
     for (uint32_t d = 0; d < nd; d++) {
-        if ((ddn[d] && craw_k_denoise(&b->direct[d].dn, &b->direct[d].dio, b->direct_shape, NULL, s) < 0) ||
+        if ((ddn[d] && craw_k_denoise(&b->direct[d].dn, &b->direct[d].dio, b->direct_shape, NULL,
+                                      b->direct[d].vio.err, s) < 0) ||
             craw_k_develop(&b->direct[d].dv, &b->direct[d].vio, 0, s) < 0)
             return CRAW_ERROR(EIO);
         b->direct_frames++;

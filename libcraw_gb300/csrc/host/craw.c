@@ -198,6 +198,13 @@ CRAW_API int craw_debug_rcd_tma(int on)
     return was;
 }
 
+CRAW_API int craw_debug_denoise_tma(int on)
+{
+    const int was = craw_k_dn_tma;
+    craw_k_dn_tma = on ? 1 : 0;
+    return was;
+}
+
 int craw_dev_alloc(CRAWContext *ctx, void **ptr, size_t bytes)
 {
     *ptr = NULL;

@@ -98,7 +98,8 @@ struct CRAWPipeline {
     uint32_t *kerr;           /* CRAW_K_ERR_* bits the kernels set */
     uint32_t *round_flags;    /* marks of the exact rounding, CRAW_K_ROUND_WORDS */
     uint32_t *round_stats;    /* its statistics, CRAW_K_ROUND_STATS_BYTES */
-    uint32_t *round_list;     /* undecided samples, CRAW_K_ROUND_LIST entries, then their count */
+    uint32_t *round_list;     /* marked, then undecided samples, CRAW_K_ROUND_LIST entries
+                               * each, then the counters */
 
     /* Plain-pipeline scratch. */
     float *p_v, *p_scratch, *p_t, *p_var;
@@ -215,7 +216,7 @@ static int time_denoise(CRAWPipeline *p, const CRAWKDenoise *k, const CRAWKDenoi
     for (int r = 0; r < 4 && ret == 0; r++) {
         float t = 0.0f;
         cudaEventRecord(e0, ctx->stream);
-        ret = craw_k_denoise(k, io, shape, NULL, ctx->stream);
+        ret = craw_k_denoise(k, io, shape, NULL, NULL, ctx->stream);
         cudaEventRecord(e1, ctx->stream);
         if (ret == 0 && cudaEventSynchronize(e1) == cudaSuccess &&
             cudaEventElapsedTime(&t, e0, e1) == cudaSuccess && r > 0 && t < *ms)
@@ -510,14 +511,14 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
         goto fail;
     if (p->has_denoise && !p->plain && (params->flags & CRAW_PIPELINE_FLAG_EXACT_ROUNDING)) {
         /* The exact rounding: its marks (a bit per sample, 2.3 MB at
-         * 5760x3240), the list of samples its float stage cannot settle
-         * (a sixteenth of the samples and their count: 4.9 MB) and its
-         * statistics. */
+         * 5760x3240), its lists of the marked samples and of those its
+         * float stage cannot settle (a sixteenth of the samples each: 9.8
+         * MB), their counters and its statistics. */
         if ((ret = craw_dev_alloc(ctx, (void **)&p->round_flags,
                                   CRAW_K_ROUND_WORDS(w / 2, h / 2) * sizeof(uint32_t))) < 0 ||
             (ret = craw_dev_alloc(ctx, (void **)&p->round_stats, CRAW_K_ROUND_STATS_BYTES)) < 0 ||
             (ret = craw_dev_alloc(ctx, (void **)&p->round_list,
-                                  (CRAW_K_ROUND_LIST(w / 2, h / 2) + 4) * sizeof(uint32_t))) < 0)
+                                  (2 * CRAW_K_ROUND_LIST(w / 2, h / 2) + 4) * sizeof(uint32_t))) < 0)
             goto fail;
         if (cudaMemsetAsync(p->round_stats, 0, CRAW_K_ROUND_STATS_BYTES, ctx->stream) != cudaSuccess) {
             ret = CRAW_ERROR(EIO);
@@ -662,7 +663,7 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
         if (exact) {
             craw_denoise_round_band(&dnk, craw_round_scale, &rd);
             rd.flags = p->round_flags;
-            rd.count2 = p->round_list + CRAW_K_ROUND_LIST(w / 2, h / 2);
+            rd.count2 = p->round_list + 2 * CRAW_K_ROUND_LIST(w / 2, h / 2);
         }
     }
 
@@ -713,7 +714,7 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
         prof_begin(&pc, ST_DENOISE);
         ret = p->plain ? craw_k_plain_denoise(&dnk, &io, p->p_t, p->p_var, s)
                        : craw_k_denoise(&dnk, &io, p->dn_shape[(dn_mode & CRAW_K_DN_HISTORY) != 0],
-                                        exact ? &rd : NULL, s);
+                                        exact ? &rd : NULL, p->kerr, s);
         prof_end(&pc);
         if (ret < 0)
             goto launch_fail;

@@ -64,8 +64,9 @@ enum CRAWKDenoiseShape {
 typedef struct CRAWKRound {
     uint32_t *flags;    /* CRAW_K_ROUND_WORDS(pw, ph) words; NULL: no marking */
     uint32_t *count2;   /* [0] the length of the list of undecided samples,
-                         * [1] the rounding's work counter: the denoise
-                         * kernel zeroes both */
+                         * [1] the rounding's work counter, [2] the number
+                         * of marked samples: the denoise kernel zeroes
+                         * all three */
     float c0, c2;
 } CRAWKRound;
 
@@ -111,20 +112,30 @@ typedef struct CRAWKDenoiseExact {
 #define CRAW_K_ROUND_RECORDS 4096
 #define CRAW_K_ROUND_STATS_BYTES (16 + 16 * CRAW_K_ROUND_RECORDS)
 
-/* Entries of the undecided-sample list, for a frame of plane size pw x ph. */
+/* Entries of each of the rounding's two lists (the marked samples, then
+ * the undecided ones), for a frame of plane size pw x ph. */
 #define CRAW_K_ROUND_LIST(pw, ph) (((size_t)4 * (pw) * (ph)) / 16 + 65536)
 
-/* rd: NULL, or the marking of samples near a code boundary. */
+/* rd: NULL, or the marking of samples near a code boundary. err: NULL,
+ * or a device word for CRAW_K_ERR_* bits. */
 int craw_k_denoise(const CRAWKDenoise *k, const CRAWKDenoiseIO *io, int shape,
-                   const CRAWKRound *rd, cudaStream_t s);
+                   const CRAWKRound *rd, uint32_t *err, cudaStream_t s);
+
+/* 1 (default): the packed spatial denoise kernels bring each interior
+ * tile's mosaic in with one TMA tile copy; 0: with plain loads
+ * (craw_debug_denoise_tma). */
+extern int craw_k_dn_tma;
 
 /* Settles the samples `rd->flags` marks (of the frame k/io describe, whose
  * denoised mosaic io->dst the denoise kernel wrote) and rewrites their
- * codes in io->dst as a double evaluation rounds them: a float decision
- * stage with a bound on its own error settles most of them; the rest
- * (rd->count2 entries of `list`, at most CRAW_K_ROUND_LIST) are evaluated
- * in double-float arithmetic. Spatial filtering without a temporal
- * history only (e->mode). */
+ * codes in io->dst as a double evaluation rounds them: the marks are
+ * gathered into a list (the first CRAW_K_ROUND_LIST entries of `list`;
+ * with more marks than that the decision stage walks the bit map
+ * instead), a float decision stage with a bound on its own error settles
+ * most of them, and the rest (rd->count2[0] entries of the second
+ * CRAW_K_ROUND_LIST entries of `list`) are evaluated in double-float
+ * arithmetic. Spatial filtering without a temporal history only
+ * (e->mode). */
 int craw_k_denoise_round(const CRAWKDenoise *k, const CRAWKDenoiseExact *e, const CRAWKDenoiseIO *io,
                          const CRAWKRound *rd, uint32_t *list, uint32_t *stats, int sm_count,
                          cudaStream_t s);

@@ -12,8 +12,8 @@
  * The denoise kernel marks the samples whose float x lies within a band
  * around a boundary (CRAWKRound). Two kernels here settle them:
  *
- * k_round_decide  takes the marked samples off the bit map (a warp's
- *   lanes share out the set bits of 32 KW words at a time) and evaluates
+ * k_round_decide  takes the marked samples off the bit map (a warp queues
+ *   the set bits of 32 KW words at a time, GA lanes a sample) and evaluates
  *   each again in float, GA lanes a sample, in a form whose error it can
  *   bound: every stabilised value of the 9x9 window as its difference from
  *   the value m_c of the code the float path chose, computed without
@@ -47,7 +47,7 @@ constexpr int NT = 128;                /* threads per CTA */
 constexpr int WIN = 9;                 /* search 3 + patch 1, both sides */
 constexpr int KW = 1;                  /* bit-map words a lane scans a step */
 constexpr int GA = 4;                  /* lanes of the decision stage a sample */
-constexpr int G = 32;                  /* lanes of the exact stage a sample */
+constexpr int G = 16;                  /* lanes of the exact stage a sample */
 constexpr float U = 0x1p-24f;          /* float unit roundoff */
 
 /* ------------------------------------------------------------ helpers */
@@ -204,19 +204,25 @@ CRAW_DEV bool decide(const CRAWKDenoise &k, const CRAWKDenoiseExact &e, const CR
     return true;
 }
 
-/* Hands out the marked samples of 32 * KW bit-map words (from `first`) to
- * the groups of GA lanes of a warp, 32 / GA at a time: fn(pl, qx, qy,
- * valid) runs on every lane (valid false in groups without a sample) so
- * that the warp stays converged. */
-template <typename F>
-CRAW_DEV void walk_marks(const uint32_t *flags, long long nwords, int ww, int ph, long long first, int lane,
-                         F &&fn)
+/* Samples a warp's decision stage takes at once: one per group of GA lanes. */
+constexpr int BATCH = 32 / GA;
+/* A warp's queue of marked samples: one step's marks (32 KW words of 32
+ * bits) on top of a partial batch. */
+constexpr int QCAP = 32 * KW * 32 + BATCH;
+
+/* Appends the marked samples of the 32 * KW bit-map words from `first` to
+ * the warp's queue Q (which holds qn) as packed indices
+ * (pl * ph + qy) * pw + qx, the list's form; returns the new length. */
+CRAW_DEV int enqueue_marks(const uint32_t *flags, long long nwords, int ww, int pw, int ph, long long first,
+                           int lane, uint32_t *Q, int qn)
 {
+    uint32_t w[KW];
     int cnt = 0;
 #pragma unroll
     for (int j = 0; j < KW; j++) {
         const long long i = first + (long long)lane * KW + j;
-        cnt += __popc(i < nwords ? __ldg(flags + i) : 0u);
+        w[j] = i < nwords ? __ldg(flags + i) : 0u;
+        cnt += __popc(w[j]);
     }
     int incl = cnt;
 #pragma unroll
@@ -226,76 +232,141 @@ CRAW_DEV void walk_marks(const uint32_t *flags, long long nwords, int ww, int ph
             incl += v;
     }
     const int tot = __shfl_sync(0xffffffffu, incl, 31);
-    const int excl = incl - cnt;
-    for (int b = 0; b < tot; b += 32 / GA) {
-        const int idx = b + lane / GA;
-        /* The lane holding entry idx: the first with incl > idx. */
-        int lo = 0, hi = 31;
+    int at = qn + incl - cnt;
 #pragma unroll
-        for (int it = 0; it < 5; it++) {
-            const int mid = (lo + hi) >> 1;
-            const int v = __shfl_sync(0xffffffffu, incl, mid);
-            if (v > idx)
-                hi = mid;
-            else
-                lo = mid + 1;
+    for (int j = 0; j < KW; j++) {
+        const long long wi = first + (long long)lane * KW + j;
+        const uint32_t row = (uint32_t)(wi / ww), base = row * (uint32_t)pw + (uint32_t)(wi % ww) * 32u;
+        for (uint32_t m = w[j]; m; m &= m - 1) {
+            const int bit = __ffs(m) - 1;
+            Q[at++] = base + (uint32_t)(bit < 16 ? 2 * bit : 2 * (bit - 16) + 1);
         }
-        const int owner = lo;
-        int kth = idx - __shfl_sync(0xffffffffu, excl, owner);
-        const bool valid = idx < tot;
-        int pl = 0, qx = 0, qy = 0;
-        if (valid) {
-            for (int j = 0; j < KW; j++) {
-                const long long wi = first + (long long)owner * KW + j;
-                uint32_t w = __ldg(flags + wi);
-                const int c = __popc(w);
-                if (kth < c) {
-                    for (int i = 0; i < kth; i++)
-                        w &= w - 1;
-                    const int bit = __ffs(w) - 1;
-                    const long long row = wi / ww;
-                    qx = (int)(wi % ww) * 32 + (bit < 16 ? 2 * bit : 2 * (bit - 16) + 1);
-                    qy = (int)(row % ph);
-                    pl = (int)(row / ph);
-                    break;
-                }
-                kth -= c;
-            }
+    }
+    __syncwarp();
+    return qn + tot;
+}
+
+/* The marked samples as a list (rd.count2[2] counts them; entries past
+ * `cap` are not written): each warp counts the marks of its own run of
+ * bit-map steps, takes its place in the list with one atomic and writes
+ * them in bit-map order, so that a batch's samples are neighbours. */
+__global__ void __launch_bounds__(NT)
+k_round_compact(const CRAWKRound rd, int pw, int ph, uint32_t *marked, uint32_t cap)
+{
+    const int lane = threadIdx.x & 31;
+    const long long warps = (long long)gridDim.x * (NT / 32);
+    const long long wid = (long long)blockIdx.x * (NT / 32) + threadIdx.x / 32;
+    const int ww = CRAW_K_ROUND_WW(pw);
+    const long long nwords = (long long)CRAW_K_ROUND_WORDS(pw, ph);
+    const long long steps = (nwords + 31) / 32, per = (steps + warps - 1) / warps;
+    const long long s0 = wid * per, s1 = s0 + per < steps ? s0 + per : steps;
+    int tot = 0;
+    for (long long st = s0; st < s1; st++) {
+        const long long i = st * 32 + lane;
+        tot += __popc(i < nwords ? __ldg(rd.flags + i) : 0u);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    if (tot == 0)
+        return;
+    uint32_t base = 0;
+    if (lane == 0)
+        base = atomicAdd(rd.count2 + 2, (uint32_t)tot);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    for (long long st = s0; st < s1; st++) {
+        const long long i = st * 32 + lane;
+        const uint32_t w = i < nwords ? __ldg(rd.flags + i) : 0u;
+        const int cnt = __popc(w);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o)
+                incl += v;
         }
-        fn(pl, qx, qy, valid);
+        uint32_t at = base + (uint32_t)(incl - cnt);
+        const uint32_t row = (uint32_t)(i / ww), first = row * (uint32_t)pw + (uint32_t)(i % ww) * 32u;
+        for (uint32_t m = w; m; m &= m - 1) {
+            const int bit = __ffs(m) - 1;
+            if (at < cap)
+                marked[at] = first + (uint32_t)(bit < 16 ? 2 * bit : 2 * (bit - 16) + 1);
+            at++;
+        }
+        base += (uint32_t)__shfl_sync(0xffffffffu, incl, 31);
     }
 }
 
+/* Decides the samples of a batch (packed indices v, one per group of GA
+ * lanes, `take` of them) and lists the undecided ones. */
+CRAW_DEV void decide_batch(const CRAWKDenoise &k, const CRAWKDenoiseExact &e, const CRAWKDenoiseIO &io,
+                           const CRAWKRound &rd, uint32_t v, int take, int g, int lane, float *D,
+                           uint32_t *list, uint32_t list_cap, uint32_t *stats)
+{
+    const bool valid = lane / GA < take;
+    if (lane == 0)
+        atomicAdd(&stats[0], (uint32_t)take);
+    const uint32_t qx = v % (uint32_t)k.pw, r = v / (uint32_t)k.pw;
+    const int qy = (int)(r % (uint32_t)k.ph), pl = (int)(r / (uint32_t)k.ph);
+    const bool done = decide(k, e, io, pl, (int)qx, qy, valid, g, lane, D, stats);
+    if (valid && !done && g == 0) {
+        const uint32_t slot = atomicAdd(rd.count2, 1u);
+        if (slot < list_cap)
+            list[slot] = v;
+    }
+}
+
+/* The decision stage over the list of marked samples: a batch of BATCH
+ * list entries a warp at a time, batches in turn over the grid's warps
+ * (their costs hardly differ). If the list overflowed (more than
+ * `marked_cap` marks), the warps walk the bit map instead: they take
+ * steps of 32 KW words off a shared counter (the marks gather where the
+ * image is bright, so fixed shares would leave a few warps with most of
+ * the work) and queue each step's marked samples, so that every batch but
+ * a warp's last fills all its groups. */
 __global__ void __launch_bounds__(NT)
 k_round_decide(const CRAWKDenoise k, const CRAWKDenoiseExact e, const CRAWKDenoiseIO io, const CRAWKRound rd,
-               uint32_t *list, uint32_t list_cap, uint32_t *stats)
+               const uint32_t *marked, uint32_t marked_cap, uint32_t *list, uint32_t list_cap,
+               uint32_t *stats)
 {
     __shared__ float Dw[NT / GA][WIN * WIN];
+    __shared__ uint32_t Qw[NT / 32][QCAP];
     const int lane = threadIdx.x & 31, g = lane % GA;
     float *D = Dw[threadIdx.x / GA];
+    const uint32_t nm = *(volatile const uint32_t *)(rd.count2 + 2);
+    if (nm <= marked_cap) {
+        const long long warps = (long long)gridDim.x * (NT / 32);
+        const long long wid = (long long)blockIdx.x * (NT / 32) + threadIdx.x / 32;
+        for (long long b = wid * BATCH; b < nm; b += warps * BATCH) {
+            const int take = nm - b < BATCH ? (int)(nm - b) : BATCH;
+            const uint32_t v = lane / GA < take ? __ldg(marked + b + lane / GA) : 0u;
+            decide_batch(k, e, io, rd, v, take, g, lane, D, list, list_cap, stats);
+        }
+        return;
+    }
+    uint32_t *Q = Qw[threadIdx.x / 32];
     const int ww = CRAW_K_ROUND_WW(k.pw);
     const long long nwords = (long long)CRAW_K_ROUND_WORDS(k.pw, k.ph);
-    /* Warps take steps of 32 KW words off a shared counter: the marks
-     * gather where the image is bright, so fixed shares would leave a few
-     * warps with most of the work. */
-    for (;;) {
-        uint32_t step = 0;
-        if (lane == 0)
-            step = atomicAdd(rd.count2 + 1, 1u);
-        const long long first = (long long)__shfl_sync(0xffffffffu, step, 0) * 32 * KW;
-        if (first >= nwords)
-            break;
-        walk_marks(rd.flags, nwords, ww, k.ph, first, lane, [&](int pl, int qx, int qy, bool valid) {
-            const uint32_t got = __ballot_sync(0xffffffffu, valid && g == 0);
-            if (lane == 0 && got)
-                atomicAdd(&stats[0], (uint32_t)__popc(got));
-            const bool done = decide(k, e, io, pl, qx, qy, valid, g, lane, D, stats);
-            if (valid && !done && g == 0) {
-                const uint32_t slot = atomicAdd(rd.count2, 1u);
-                if (slot < list_cap)
-                    list[slot] = ((uint32_t)pl * (uint32_t)k.ph + (uint32_t)qy) * (uint32_t)k.pw + (uint32_t)qx;
-            }
-        });
+    int qn = 0;               /* the same on every lane, as is `more` */
+    bool more = true;
+    while (more || qn > 0) {
+        if (more) {
+            uint32_t c = 0;
+            if (lane == 0)
+                c = atomicAdd(rd.count2 + 1, 1u);
+            const long long first = (long long)__shfl_sync(0xffffffffu, c, 0) * 32 * KW;
+            if (first >= nwords)
+                more = false;
+            else
+                qn = enqueue_marks(rd.flags, nwords, ww, k.pw, k.ph, first, lane, Q, qn);
+        }
+        while (qn >= BATCH || (!more && qn > 0)) {
+            const int take = qn < BATCH ? qn : BATCH;
+            const uint32_t v = lane / GA < take ? Q[qn - take + lane / GA] : 0u;
+            __syncwarp();   /* read before the next steps write over it */
+            qn -= take;
+            decide_batch(k, e, io, rd, v, take, g, lane, D, list, list_cap, stats);
+        }
     }
 }
 
@@ -433,12 +504,17 @@ extern "C" int craw_k_denoise_round(const CRAWKDenoise *k, const CRAWKDenoiseExa
         return -5;
     const int sms = sm_count > 0 ? sm_count : 152;
     const size_t cap = CRAW_K_ROUND_LIST(k->pw, k->ph);
-    const long long steps = ((long long)CRAW_K_ROUND_WORDS(k->pw, k->ph) + 32 * KW - 1) / (32 * KW);
-    long long ctas_a = (steps + NT / 32 - 1) / (NT / 32);
-    ctas_a = ctas_a < (long long)sms * 12 ? ctas_a : (long long)sms * 12;
-    k_round_decide<<<(unsigned)(ctas_a > 0 ? ctas_a : 1), NT, 0, s>>>(*k, *e, *io, *rd, list, (uint32_t)cap, stats);
+    uint32_t *marked = list, *undecided = list + cap;
+    const long long steps = ((long long)CRAW_K_ROUND_WORDS(k->pw, k->ph) + 31) / 32;
+    long long ctas_c = (steps / 4 + NT / 32 - 1) / (NT / 32);
+    ctas_c = ctas_c < (long long)sms * 8 ? ctas_c : (long long)sms * 8;
+    k_round_compact<<<(unsigned)(ctas_c > 0 ? ctas_c : 1), NT, 0, s>>>(*rd, k->pw, k->ph, marked, (uint32_t)cap);
     if (cudaGetLastError() != cudaSuccess)
         return -5;
-    k_round_exact<<<(unsigned)sms * 8, NT, 0, s>>>(*e, *io, *rd, list, (uint32_t)cap, stats);
+    k_round_decide<<<(unsigned)sms * 8, NT, 0, s>>>(*k, *e, *io, *rd, marked, (uint32_t)cap, undecided,
+                                                    (uint32_t)cap, stats);
+    if (cudaGetLastError() != cudaSuccess)
+        return -5;
+    k_round_exact<<<(unsigned)sms * 8, NT, 0, s>>>(*e, *io, *rd, undecided, (uint32_t)cap, stats);
     return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }

@@ -25,6 +25,7 @@
 #include <stdint.h>
 
 #include "common.cuh"
+#include "tma.cuh"
 
 namespace craw_dn {
 
@@ -91,7 +92,8 @@ CRAW_DEV void load_quad_f32(const float *base, size_t pitch, int qx, int qy, flo
 /* STAGED: the tile's raw mosaic and its output pass through shared memory
  * (below); the batch's persistent kernel leaves it off, whose shared
  * memory would otherwise cost it a CTA an SM. */
-template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2 = false, bool STAGED = true>
+template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2 = false, bool STAGED = true,
+          bool TMA = false>
 struct Cfg {
     static constexpr int R = SPATIAL ? S + P : 0;       /* apron of the tile */
     static constexpr int OX = 16 * BW, OY = 2 * M * WP;  /* plane samples per tile */
@@ -118,7 +120,13 @@ struct Cfg {
     static constexpr int RW_W = 2 * OX, RW_H = 2 * OY;
     static constexpr int RW_OFF = BASE_FLOATS;
     static_assert(RW_OFF % 4 == 0 && RW_W % 8 == 0, "16-byte rows");
-    static constexpr int smem_floats = BASE_FLOATS + (STAGED ? RW_W * RW_H / 2 : 0);
+    /* TMA (spatial filtering only): the mosaic region of the tile and its
+     * apron, 2 TX x 2 TY samples, as one tile copy leaves it, after the
+     * rest (with room to align it to 128 bytes). */
+    static constexpr int BOX_W = 2 * TX, BOX_H = 2 * TY;
+    static constexpr uint32_t BOX_BYTES = BOX_W * BOX_H * 2;
+    static constexpr int BOX_OFF = BASE_FLOATS + (STAGED ? RW_W * RW_H / 2 : 0);
+    static constexpr int smem_floats = BOX_OFF + (TMA ? (int)BOX_BYTES / 4 + 32 : 0);
 };
 
 /* The NLM search of one thread: BW columns x M rows of one plane, at the
@@ -376,11 +384,12 @@ struct SearchX2 {
  * their float error about 3x smaller at a boundary and the marked band
  * narrower, for about 6 % more time in the search. */
 template <int BW, int M, int WP, bool SPATIAL, bool TEMPORAL, bool HISTORY, bool X2 = false, bool STAGED = true,
-          bool MARK = false>
+          bool MARK = false, bool TMA = false>
 CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int bx, int by, float *smem,
-                           const CRAWKRound *rd = nullptr)
+                           const CRAWKRound *rd = nullptr, const CUtensorMap *tmap = nullptr,
+                           uint32_t *err = nullptr)
 {
-    using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2, STAGED>;
+    using C = Cfg<BW, M, WP, SPATIAL, TEMPORAL, HISTORY, X2, STAGED, TMA>;
     static_assert(!C::PACKED || BW == 2, "the packed search pairs a thread's two columns");
     constexpr int R = C::R, OX = C::OX, OY = C::OY, TX = C::TX, TY = C::TY, TS = C::TS;
     constexpr int NT = C::NT;
@@ -395,17 +404,53 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
     if (MARK && rd->count2 && bx == 0 && by == 0 && tid == 0) {
         rd->count2[0] = 0;      /* this frame's list of undecided samples starts empty */
         rd->count2[1] = 0;      /* and so does the rounding's work counter */
+        rd->count2[2] = 0;      /* and its list of marked samples */
     }
 
     /* ---- fill: the stabilised tile, temporally averaged when there is a
      * history (reference lib/ref/ref_denoise.c:244-296). */
     uint32_t *raw32 = reinterpret_cast<uint32_t *>(smem + C::RW_OFF);
     if constexpr (!HISTORY) {
+        /* TMA: a tile whose apron lies inside the frame (plane columns
+         * tx0 - R .. tx0 - R + TX, rows ty0 - R .. ty0 - R + TY) brings its
+         * mosaic region in with one tile copy; the others, at the frame's
+         * edges, mirror their plain loads. */
+        const uint32_t *box = nullptr;
+        if constexpr (TMA) {
+            static_assert(SPATIAL && !TEMPORAL, "the spatial fill");
+            static_assert((2 * OX) % 8 == 0 && (2 * R) % 8 == 0 && (C::BOX_W * 2) % 16 == 0,
+                          "every box starts and ends on a 16-byte boundary");
+            __shared__ __align__(8) uint64_t tma_bar;
+            if (tx0 >= R && ty0 >= R && tx0 - R + TX <= k.pw && ty0 - R + TY <= k.ph) {
+                box = reinterpret_cast<const uint32_t *>(((uintptr_t)(smem + C::BOX_OFF) + 127) &
+                                                         ~(uintptr_t)127);
+                craw_tma::bar_init(&tma_bar);
+                if (tid == 0)
+                    craw_tma::load_2d((void *)box, tmap, 2 * (tx0 - R), 2 * (ty0 - R), &tma_bar, C::BOX_BYTES);
+                if (!__syncthreads_and(craw_tma::wait(&tma_bar, 0))) {
+                    /* Never expected: record it, give the copy one more
+                     * bound to land before the CTA leaves, and skip the
+                     * tile. */
+                    if (tid == 0 && err)
+                        atomicOr(err, CRAW_K_ERR_TMA_WAIT);
+                    (void)craw_tma::wait(&tma_bar, 0);
+                    return;
+                }
+            }
+        }
         for (int i = tid; i < TX * TY; i += NT) {
             int r = i / TX, c = i % TX;
-            int qy = craw_mirror(ty0 - R + r, k.ph), qx = craw_mirror(tx0 - R + c, k.pw);
             uint32_t q[4], qa, qb;
-            load_quad_u16(io, qx, qy, q, qa, qb);
+            if (TMA && box) {
+                /* Plane row r is box rows 2r, 2r + 1; quad column c is the
+                 * box's 32-bit word c of each. */
+                qa = box[(2 * r) * TX + c];
+                qb = box[(2 * r + 1) * TX + c];
+                q[0] = qa & 0xffffu; q[1] = qa >> 16; q[2] = qb & 0xffffu; q[3] = qb >> 16;
+            } else {
+                int qy = craw_mirror(ty0 - R + r, k.ph), qx = craw_mirror(tx0 - R + c, k.pw);
+                load_quad_u16(io, qx, qy, q, qa, qb);
+            }
             if constexpr (STAGED)
                 keep_raw<OX, OY>(raw32, r - R, c - R, qa, qb);
 #pragma unroll

@@ -8,6 +8,7 @@
 #include <stdint.h>
 
 #include "develop_tile.cuh"
+#include "tma.cuh"
 
 /* Whether the RCD interior tiles load their mosaic by TMA (1, the
  * default) or by plain loads (0, for comparison and tests). */
@@ -79,27 +80,6 @@ k_develop_rcd_quads(const CRAWKDevelop k, const CRAWKDevelopIO io, const QuadGri
  * two columns (read as zeros and never used). */
 constexpr int kBoxW = QTW + 16, kBoxH = QTH + 12;
 constexpr uint32_t kBoxBytes = kBoxW * kBoxH * 2;
-/* try_wait suspends for a while each time; this bound is seconds. */
-constexpr int kWaitTries = 1 << 20;
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p)
-{
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity)
-{
-    for (int i = 0; i < kWaitTries; i++) {
-        uint32_t done;
-        asm volatile("{\n\t.reg .pred p;\n\t"
-                     "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-                     "selp.u32 %0, 1, 0, p;\n\t}"
-                     : "=r"(done) : "r"(bar), "r"(parity) : "memory");
-        if (done)
-            return true;
-    }
-    return false;
-}
 
 __global__ void __launch_bounds__(QNT)
 k_develop_rcd_quads_tma(const CRAWKDevelop k, const CRAWKDevelopIO io, const QuadGrid g,
@@ -114,80 +94,21 @@ k_develop_rcd_quads_tma(const CRAWKDevelop k, const CRAWKDevelopIO io, const Qua
      * first writes after the load; 128-byte aligned for the copy. */
     static_assert(kBoxBytes + 128 <= 4 * RcdQuads<QTW, QTH, QNT>::DN * sizeof(float), "box fits");
     uint32_t *box = reinterpret_cast<uint32_t *>(((uintptr_t)t.Dp + 127) & ~(uintptr_t)127);
-    const uint32_t bar = smem_u32(&bar_s);
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(bar) : "memory");
-        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
-                     :: "r"(bar), "r"(kBoxBytes) : "memory");
-        asm volatile("cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
-                     " [%0], [%1, {%2, %3}], [%4];"
-                     :: "r"(smem_u32(box)), "l"(reinterpret_cast<uint64_t>(&tmap)), "r"(x0 - 8), "r"(y0 - 6),
-                        "r"(bar)
-                     : "memory");
-    }
-    if (!mbar_wait(bar, 0)) {
+    craw_tma::bar_init(&bar_s);
+    if (threadIdx.x == 0)
+        craw_tma::load_2d(box, &tmap, x0 - 8, y0 - 6, &bar_s, kBoxBytes);
+    if (!__syncthreads_and(craw_tma::wait(&bar_s, 0))) {
         /* Never expected: record it, give the copy one more bound to land
          * before the CTA leaves, and skip the tile. */
         if (threadIdx.x == 0 && io.err)
             atomicOr(io.err, CRAW_K_ERR_TMA_WAIT);
-        (void)mbar_wait(bar, 0);
+        (void)craw_tma::wait(&bar_s, 0);
         return;
     }
     t.load_box<kBoxW>(k, io, box);
     __syncthreads();
     t.run();
     epilogue<QTW, QTH, QNT>(k, io, x0, y0, t.rgb);
-}
-
-/* The tensor map of a mosaic (16-bit samples, pitch in bytes) for the
- * box above; the last one a thread encoded is kept. False where the
- * driver call is not available or refuses the layout. */
-typedef CUresult (*EncodeTiled)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
-                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
-                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-bool mosaic_tmap(const void *src, size_t pitch, int w, int h, CUtensorMap *out)
-{
-    /* Looked up once per process (a thread-safe static initialisation). */
-    static const EncodeTiled encode = [] {
-        void *fn = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        EncodeTiled e = nullptr;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess && q == cudaDriverEntryPointSuccess)
-            e = reinterpret_cast<EncodeTiled>(fn);
-        (void)cudaGetLastError();
-        return e;
-    }();
-    thread_local const void *c_src = nullptr;
-    thread_local size_t c_pitch = 0;
-    thread_local int c_w = 0, c_h = 0;
-    thread_local CUtensorMap c_map;
-    if (!encode || ((uintptr_t)src & 15) || (pitch & 15))
-        return false;
-    if (src != c_src || pitch != c_pitch || w != c_w || h != c_h) {
-        const cuuint64_t dims[2] = { (cuuint64_t)w, (cuuint64_t)h };
-        const cuuint64_t strides[1] = { (cuuint64_t)pitch };
-        const cuuint32_t box[2] = { (cuuint32_t)kBoxW, (cuuint32_t)kBoxH };
-        const cuuint32_t estr[2] = { 1, 1 };
-        if (encode(&c_map, CU_TENSOR_MAP_DATA_TYPE_UINT16, 2, const_cast<void *>(src), dims, strides, box, estr,
-                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS) {
-            c_src = nullptr;
-            return false;
-        }
-        c_src = src;
-        c_pitch = pitch;
-        c_w = w;
-        c_h = h;
-    }
-    *out = c_map;
-    return true;
 }
 
 /* The per-pixel RCD on the ring of border quad tiles, BTW x BTH pixels a
@@ -236,7 +157,7 @@ int launch_rcd(const CRAWKDevelop *k, const CRAWKDevelopIO *io, cudaStream_t s)
     if (g.interior_x() > 0 && g.interior_y() > 0) {
         const dim3 grid(g.interior_x(), g.interior_y());
         CUtensorMap tmap;
-        if (craw_k_rcd_tma && mosaic_tmap(io->src, io->src_pitch, k->width, k->height, &tmap))
+        if (craw_k_rcd_tma && craw_tmap_u16(io->src, io->src_pitch, k->width, k->height, kBoxW, kBoxH, &tmap))
             k_develop_rcd_quads_tma<<<grid, QNT, smem, s>>>(*k, *io, g, tmap);
         else
             k_develop_rcd_quads<<<grid, QNT, smem, s>>>(*k, *io, g);
