@@ -83,6 +83,7 @@ struct CRAWPipeline {
     size_t hl_pitch;
     void *hl_levels;            /* the colour field's pyramid */
     int dn_shape[2], dev_shape;   /* denoise tile shape without / with a history */
+    bool tune_held;              /* holds its size's autotuner cache entry */
 
     /* Device memory. */
     uint16_t *clean;  size_t clean_pitch;
@@ -144,9 +145,12 @@ static int alloc_pitched(CRAWPipeline *p, void **ptr, size_t *pitch, size_t row_
     return craw_dev_alloc(p->ctx, ptr, pt * rows);
 }
 
+static void tune_release(CRAWPipeline *p);
+
 static void release(CRAWPipeline *p)
 {
     CRAWContext *ctx = p->ctx;
+    tune_release(p);
     void *bufs[] = {
         p->clean, p->lvl[0], p->lvl[1], p->var[0], p->var[1], p->inter, p->q, p->qf,
         p->awb_rec, p->awb_dev, p->kerr, p->p_v, p->p_scratch, p->p_t, p->p_var,
@@ -174,29 +178,62 @@ static void release(CRAWPipeline *p)
  * scratch mosaic (the filter's work does not depend on the data), and
  * remembered for the process (each of the two on its own) so that every
  * later pipeline of the same size starts at once with the same shapes:
- * pipelines of one size give the same results. */
-#define TUNE_CACHE 32
+ * pipelines of one size give the same results. An entry is held while a
+ * pipeline of its size exists, so its shapes stay those of every live
+ * pipeline of that size; when the table is full, the least recently used
+ * entry that no pipeline holds makes room. */
+#define TUNE_CACHE 256
 static struct tune_entry {
     uint32_t w, h;
     int shape[2];
     bool known[2];
+    uint32_t live;               /* pipelines of this size holding the entry */
+    uint64_t used;               /* tick of the last lookup */
 } tune_cache[TUNE_CACHE];
 static int tune_nb;
+static uint64_t tune_tick;
 static pthread_mutex_t tune_lock = PTHREAD_MUTEX_INITIALIZER;
 
-/* The cache entry of a size, created if there is room; NULL otherwise.
- * Called with tune_lock held. */
+/* The cache entry of a size, created if asked and there is room (a free
+ * slot, or the least recently used entry no pipeline holds); NULL
+ * otherwise. Called with tune_lock held. */
 static struct tune_entry *tune_entry(uint32_t w, uint32_t h, bool create)
 {
+    struct tune_entry *e = NULL;
     for (int i = 0; i < tune_nb; i++)
-        if (tune_cache[i].w == w && tune_cache[i].h == h)
+        if (tune_cache[i].w == w && tune_cache[i].h == h) {
+            tune_cache[i].used = ++tune_tick;
             return &tune_cache[i];
-    if (!create || tune_nb == TUNE_CACHE)
+        }
+    if (!create)
         return NULL;
-    memset(&tune_cache[tune_nb], 0, sizeof(tune_cache[0]));
-    tune_cache[tune_nb].w = w;
-    tune_cache[tune_nb].h = h;
-    return &tune_cache[tune_nb++];
+    if (tune_nb < TUNE_CACHE) {
+        e = &tune_cache[tune_nb++];
+    } else {
+        for (int i = 0; i < TUNE_CACHE; i++)
+            if (!tune_cache[i].live && (!e || tune_cache[i].used < e->used))
+                e = &tune_cache[i];
+        if (!e)
+            return NULL;
+    }
+    memset(e, 0, sizeof(*e));
+    e->w = w;
+    e->h = h;
+    e->used = ++tune_tick;
+    return e;
+}
+
+/* Lets go of the cache entry a pipeline holds. */
+static void tune_release(CRAWPipeline *p)
+{
+    struct tune_entry *e;
+    if (!p->tune_held)
+        return;
+    pthread_mutex_lock(&tune_lock);
+    if ((e = tune_entry(p->params.width, p->params.height, false)) && e->live)
+        e->live--;
+    pthread_mutex_unlock(&tune_lock);
+    p->tune_held = false;
 }
 
 static int time_denoise(CRAWPipeline *p, const CRAWKDenoise *k, const CRAWKDenoiseIO *io, int shape,
@@ -239,13 +276,20 @@ static int autotune(CRAWPipeline *p)
     bool need[2] = { p->has_denoise, p->has_temporal };
     struct tune_entry *e;
 
+    const bool want[2] = { need[0], need[1] };
+
     pthread_mutex_lock(&tune_lock);
-    if ((e = tune_entry(w, h, false)))
+    if ((e = tune_entry(w, h, false))) {
         for (int hist = 0; hist < 2; hist++)
             if (need[hist] && e->known[hist]) {
                 p->dn_shape[hist] = e->shape[hist];
                 need[hist] = false;
             }
+        if (!need[0] && !need[1]) {
+            e->live++;
+            p->tune_held = true;
+        }
+    }
     pthread_mutex_unlock(&tune_lock);
     if (!need[0] && !need[1])
         return 0;
@@ -294,9 +338,9 @@ static int autotune(CRAWPipeline *p)
     /* Another thread may have tuned the same size meanwhile: its shapes
      * win, so that every pipeline of the size agrees. */
     pthread_mutex_lock(&tune_lock);
-    if ((e = tune_entry(w, h, true)))
+    if (ret == 0 && (e = tune_entry(w, h, true))) {
         for (int hist = 0; hist < 2; hist++) {
-            if (!need[hist])
+            if (!want[hist])
                 continue;
             if (e->known[hist]) {
                 p->dn_shape[hist] = e->shape[hist];
@@ -305,6 +349,9 @@ static int autotune(CRAWPipeline *p)
                 e->known[hist] = true;
             }
         }
+        e->live++;
+        p->tune_held = true;
+    }
     pthread_mutex_unlock(&tune_lock);
 done:
     craw_dev_free(ctx, mosaic);

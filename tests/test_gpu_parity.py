@@ -195,6 +195,24 @@ def test_autotuned_shapes_agree_per_size(ctx):
     assert len(spatial) == 1 and len(temporal) == 1, seen
 
 
+def test_autotuned_shapes_survive_many_sizes(ctx):
+    """A size's shapes stay those of its live pipelines however many other
+    sizes are tuned meanwhile (the tuner's table keeps an entry while a
+    pipeline of its size exists), and a later pipeline of the size after
+    the others finds them too."""
+    w, h = 1030, 614
+    flags = L.FLAG_DENOISE | L.FLAG_TEMPORAL_DENOISE
+    with L.Pipeline(ctx, L.pipeline_params(w, h, flags=flags)) as held:
+        first = held.kernel_config()
+        for i in range(48):
+            with L.Pipeline(ctx, L.pipeline_params(64 + 2 * i, 34, flags=flags)):
+                pass
+        with L.Pipeline(ctx, L.pipeline_params(w, h, flags=flags)) as again:
+            assert again.kernel_config() == first
+    with L.Pipeline(ctx, L.pipeline_params(w, h, flags=flags)) as later:
+        assert later.kernel_config() == first
+
+
 @pytest.mark.parametrize("storage", [L.STORAGE_FP32, L.STORAGE_FP16])
 @pytest.mark.parametrize("deb", [L.DEBAYER_BILINEAR, L.DEBAYER_RCD])
 @pytest.mark.parametrize("chroma", [False, True])
