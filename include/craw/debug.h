@@ -22,6 +22,14 @@ CRAW_API int craw_debug_force_denoise_shape(int shape);
  * comparing the two. Returns the previous setting. */
 CRAW_API int craw_debug_rcd_tma(int on);
 
+/* How the RCD's interior runs: 0 by 64x16 tiles; 1 (the default) by
+ * strips (a thread a quad column, walking down the frame) unless the
+ * colour stage has the ACES gamut compression, where the tiles are the
+ * faster; 2 by strips wherever they apply; for comparing the two (they
+ * give the same bits). Another value only reads. Returns the previous
+ * setting. */
+CRAW_API int craw_debug_rcd_strips(int mode);
+
 /* 1 (default): the denoise's interior tiles (packed kernels, spatial
  * filtering) bring their mosaic region into shared memory with one TMA
  * tile copy each; 0: with plain loads, for comparing the two. Returns the

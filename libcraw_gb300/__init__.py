@@ -282,7 +282,7 @@ for _s, _n in ((Profile, 1264), (FrameParams, 264), (PipelineParams, 256), (Cuda
 EXPORTS = (
     "craw_version_int", "craw_log", "craw_context_create", "craw_context_free",
     "craw_cuda_check_device", "craw_debug_fail_alloc", "craw_debug_force_denoise_shape",
-    "craw_debug_rcd_tma", "craw_debug_denoise_tma", "craw_debug_kernel_errors", "craw_debug_denoise_round",
+    "craw_debug_rcd_tma", "craw_debug_rcd_strips", "craw_debug_denoise_tma", "craw_debug_kernel_errors", "craw_debug_denoise_round",
     "craw_debug_denoise_round_decide", "craw_debug_denoise_round_stats",
     "craw_pipeline_params_init", "craw_frame_params_init", "craw_pipeline_create",
     "craw_pipeline_free", "craw_pipeline_record", "craw_pipeline_get_awb_histogram",
@@ -364,6 +364,7 @@ def lib() -> C.CDLL:
         "craw_debug_fail_alloc": (None, [i32]),
         "craw_debug_force_denoise_shape": (i32, [i32]),
         "craw_debug_rcd_tma": (i32, [i32]),
+        "craw_debug_rcd_strips": (i32, [i32]),
         "craw_debug_denoise_tma": (i32, [i32]),
         "craw_debug_kernel_errors": (i32, [vp]),
         "craw_debug_denoise_round": (C.c_float, [C.c_float]),
@@ -916,6 +917,13 @@ def debug_rcd_tma(on: bool) -> bool:
     """RCD interior tiles by one TMA tile copy (True, the default) or by
     plain loads; returns the previous setting."""
     return bool(lib().craw_debug_rcd_tma(1 if on else 0))
+
+
+def debug_rcd_strips(mode: int) -> int:
+    """RCD interior by 64x16 tiles (0), by strips unless the colour stage
+    has the gamut compression (1, the default), or by strips wherever they
+    apply (2); -1 only reads. Returns the previous setting."""
+    return int(lib().craw_debug_rcd_strips(int(mode)))
 
 
 def debug_denoise_tma(on: bool) -> bool:

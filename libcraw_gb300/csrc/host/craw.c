@@ -198,6 +198,14 @@ CRAW_API int craw_debug_rcd_tma(int on)
     return was;
 }
 
+CRAW_API int craw_debug_rcd_strips(int mode)
+{
+    const int was = craw_k_rcd_strips;
+    if (mode >= 0 && mode <= 2)
+        craw_k_rcd_strips = mode;
+    return was;
+}
+
 CRAW_API int craw_debug_denoise_tma(int on)
 {
     const int was = craw_k_dn_tma;

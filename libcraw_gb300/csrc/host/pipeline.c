@@ -600,6 +600,10 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
     }
     if ((ret = craw_dev_sync(ctx)) < 0)
         goto fail;
+    if (!p->plain && craw_k_develop_prepare(params->debayer) < 0) {
+        ret = CRAW_ERROR(EIO);
+        goto fail;
+    }
     if (craw_forced_denoise_shape >= 0) {
         p->dn_shape[0] = p->dn_shape[1] = craw_forced_denoise_shape;
     } else if ((p->has_denoise || p->has_temporal) && !p->plain &&

@@ -211,9 +211,20 @@ typedef struct CRAWKDevelopIO {
 int craw_k_develop(const CRAWKDevelop *k, const CRAWKDevelopIO *io, int shape,
                    cudaStream_t s);
 
+/* Readies the develop kernels of a debayer method on the current device
+ * (their launch attributes, which also loads them): called when a
+ * pipeline is created, so that its first frame starts at once. 0 or -5. */
+int craw_k_develop_prepare(int method);
+
 /* 1 (default): the RCD's interior tiles bring their mosaic in with one TMA
  * tile copy; 0: with plain loads (craw_debug_rcd_tma). */
 extern int craw_k_rcd_tma;
+
+/* The RCD's interior by 64x16 tiles (0), by strips (one quad column a
+ * thread walking down a segment of quad rows) unless the colour stage
+ * has the gamut compression (1, the default), or by strips wherever they
+ * apply (2): craw_debug_rcd_strips. The two give the same bits. */
+extern int craw_k_rcd_strips;
 
 /* ------------------------------------------------------------- chroma */
 

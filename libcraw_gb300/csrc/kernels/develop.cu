@@ -7,13 +7,17 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "develop_strip.cuh"
 #include "develop_tile.cuh"
 #include "tma.cuh"
 
 /* Whether the RCD interior tiles load their mosaic by TMA (1, the
- * default) or by plain loads (0, for comparison and tests). */
+ * default) or by plain loads (0, for comparison and tests); whether the
+ * interior runs by 64x16 tiles (0), by strips where they are the faster
+ * (1, the default) or by strips wherever they apply (2). */
 extern "C" {
 int craw_k_rcd_tma = 1;
+int craw_k_rcd_strips = 1;
 }
 
 namespace {
@@ -111,6 +115,15 @@ k_develop_rcd_quads_tma(const CRAWKDevelop k, const CRAWKDevelopIO io, const Qua
     epilogue<QTW, QTH, QNT>(k, io, x0, y0, t.rgb);
 }
 
+/* The interior by strips (develop_strip.cuh): SOUT x seg output quads a
+ * CTA, four CTAs an SM (55 KB of shared memory each). */
+__global__ void __launch_bounds__(SNT, 4)
+k_develop_rcd_strips(const CRAWKDevelop k, const CRAWKDevelopIO io, const StripGrid g)
+{
+    extern __shared__ __align__(16) float smem[];
+    rcd_strip(k, io, g, blockIdx.x, blockIdx.y, *reinterpret_cast<StripSmem *>(smem));
+}
+
 /* The per-pixel RCD on the ring of border quad tiles, BTW x BTH pixels a
  * CTA (QTW / BTW of them a quad tile). */
 __global__ void __launch_bounds__(256, 8)
@@ -145,16 +158,69 @@ int launch(const CRAWKDevelop *k, const CRAWKDevelopIO *io, cudaStream_t s)
     return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }
 
+/* The current device's SM count, kept per device ordinal below 64 (152,
+ * GB300's, if the query fails). */
+int craw_sm_count()
+{
+    static std::atomic<int> known[64];
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return 152;
+    if (dev >= 0 && dev < 64 && (sms = known[dev].load(std::memory_order_relaxed)) > 0)
+        return sms;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+        return 152;
+    if (dev >= 0 && dev < 64)
+        known[dev].store(sms, std::memory_order_relaxed);
+    return sms;
+}
+
+/* The RCD kernels' shared-memory sizes, set once per device; this also
+ * loads them, so that a pipeline's first frame does not wait for it. */
+int prepare_rcd()
+{
+    constexpr size_t smem = RcdQuads<QTW, QTH, QNT>::floats * sizeof(float);
+    static std::atomic<uint64_t> attr_plain{ 0 }, attr_tma{ 0 }, attr_strips{ 0 };
+    if (craw_smem_attr(k_develop_rcd_quads, smem, attr_plain) < 0 ||
+        craw_smem_attr(k_develop_rcd_quads_tma, smem, attr_tma) < 0 ||
+        craw_smem_attr(k_develop_rcd_strips, sizeof(StripSmem), attr_strips) < 0)
+        return -5;
+    return 0;
+}
+
 int launch_rcd(const CRAWKDevelop *k, const CRAWKDevelopIO *io, cudaStream_t s)
 {
     constexpr size_t smem = RcdQuads<QTW, QTH, QNT>::floats * sizeof(float);
-    static std::atomic<uint64_t> attr_plain{ 0 }, attr_tma{ 0 };
-    if (craw_smem_attr(k_develop_rcd_quads, smem, attr_plain) < 0 ||
-        craw_smem_attr(k_develop_rcd_quads_tma, smem, attr_tma) < 0)
+    if (prepare_rcd() < 0)
         return -5;
     QuadGrid g;
     g.init(k->width, k->height);
-    if (g.interior_x() > 0 && g.interior_y() > 0) {
+    /* Strips unless the colour stage carries the gamut compression (its
+     * long chains of MUFU work sit in front of every step's barrier with
+     * 16 warps an SM to hide them: the strips take 0.260 ms against the
+     * tiles' 0.255 ms at 5760x3240 with it, 0.213 against 0.250 without),
+     * or the chroma path (the tiles' epilogue writes its block means). */
+    const bool strips = craw_k_rcd_strips == 2 ||
+                        (craw_k_rcd_strips == 1 && !(k->color.flags & CRAW_K_COLOR_RGC));
+    if (g.interior_x() > 0 && g.interior_y() > 0 && strips && !io->quarter) {
+        /* The interior tiles' region as strips. */
+        StripGrid sg;
+        sg.qx0 = g.c_lo * (QTW / 2);
+        sg.nqx = g.interior_x() * (QTW / 2);
+        sg.qy0 = g.r_lo * (QTH / 2);
+        sg.nqy = g.interior_y() * (QTH / 2);
+        /* Segments as tall as one wave of four CTAs an SM allows (a taller
+         * segment recomputes less of its passes' first rows), at least 8
+         * quad rows. */
+        const int gx = (sg.nqx + SOUT - 1) / SOUT;
+        const int nseg = (4 * craw_sm_count()) / gx > 1 ? (4 * craw_sm_count()) / gx : 1;
+        sg.seg = 4 * ((sg.nqy / 4 + nseg - 1) / nseg);
+        sg.seg = sg.seg < 8 ? 8 : sg.seg;
+        const dim3 grid(gx, (sg.nqy + sg.seg - 1) / sg.seg);
+        k_develop_rcd_strips<<<grid, SNT, sizeof(StripSmem), s>>>(*k, *io, sg);
+        if (cudaGetLastError() != cudaSuccess)
+            return -5;
+    } else if (g.interior_x() > 0 && g.interior_y() > 0) {
         const dim3 grid(g.interior_x(), g.interior_y());
         CUtensorMap tmap;
         if (craw_k_rcd_tma && craw_tmap_u16(io->src, io->src_pitch, k->width, k->height, kBoxW, kBoxH, &tmap))
@@ -174,6 +240,14 @@ int launch_rcd(const CRAWKDevelop *k, const CRAWKDevelopIO *io, cudaStream_t s)
 }
 
 } // namespace
+
+extern "C" int craw_k_develop_prepare(int method)
+{
+    (void)craw_sm_count();
+    if (method == kRcd)
+        return prepare_rcd();
+    return 0;
+}
 
 extern "C" int craw_k_develop(const CRAWKDevelop *k, const CRAWKDevelopIO *io, int shape,
                               cudaStream_t s)

@@ -267,6 +267,114 @@ struct RcdTile {
     }
 };
 
+/* ------------------------------------------- RCD arithmetic of the quads */
+
+/* The RCD formulas of reference lib/ref/ref_debayer.c:204-395 as the quad
+ * forms (tiles and strips) evaluate them, every rounding explicit, so that
+ * both give the same bits whatever the compiler contracts around them. */
+
+/* 1/x on the MUFU (x >= 1e-5 wherever it is used: no denormals). */
+CRAW_DEV float rq_rcp(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+/* 1 + (a - b) / (a + b + eps) for low passes a, b already clamped at 0
+ * (the reference clamps them where it forms the ratio; they are stored
+ * clamped, which they are used for only). */
+CRAW_DEV float rq_ratio1(float a, float b)
+{
+    return __fmaf_rn(__fsub_rn(a, b), rq_rcp(__fadd_rn(__fadd_rn(a, b), RCD_EPS)), 1.0f);
+}
+
+/* The low pass at a site from its 3x3 window (n, s, w, e: the cross; the
+ * four diagonals), clamped at 0 for the ratios it feeds. */
+CRAW_DEV float rq_lowpass(float c, float n, float s, float w, float e, float nw, float ne, float sw, float se)
+{
+    float t = __fmaf_rn(4.0f, c, __fmul_rn(2.0f, __fadd_rn(__fadd_rn(__fadd_rn(n, s), w), e)));
+    t = __fadd_rn(__fadd_rn(__fadd_rn(__fadd_rn(t, nw), ne), sw), se);
+    return fmaxf(__fmul_rn(t, 1.0f / 16.0f), 0.0f);
+}
+
+/* One discrimination: |a1 - b1| + |2c - a2 - b2| (c2 = 2c). */
+CRAW_DEV float rq_disc(float c2, float a1, float b1, float a2, float b2)
+{
+    return __fadd_rn(fabsf(__fsub_rn(a1, b1)), fabsf(__fsub_rn(__fsub_rn(c2, a2), b2)));
+}
+
+/* The (V, H, P, Q) discriminations of the site at the centre of a 5x5
+ * window, w[r][c] for r, c in 0..4. */
+template <typename WIN>
+CRAW_DEV float4 rq_disc4(const WIN &w)
+{
+    const float c2 = __fmul_rn(2.0f, w(2, 2));
+    float4 d;
+    d.x = rq_disc(c2, w(1, 2), w(3, 2), w(0, 2), w(4, 2));
+    d.y = rq_disc(c2, w(2, 1), w(2, 3), w(2, 0), w(2, 4));
+    d.z = rq_disc(c2, w(3, 1), w(1, 3), w(4, 0), w(0, 4));
+    d.w = rq_disc(c2, w(1, 1), w(3, 3), w(0, 0), w(4, 4));
+    return d;
+}
+
+CRAW_DEV float4 rq_add4(float4 a, float4 b)
+{
+    return make_float4(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z), __fadd_rn(a.w, b.w));
+}
+
+/* The vertical weight from the 3x3 sums of (V, H, P, Q), and the diagonal
+ * one. */
+CRAW_DEV float rq_wv(float4 s)
+{
+    const float vs = __fmul_rn(s.x, 1.0f / 9.0f), hs = __fmul_rn(s.y, 1.0f / 9.0f);
+    return __fmul_rn(hs, rq_rcp(__fadd_rn(__fadd_rn(hs, vs), RCD_EPS)));
+}
+CRAW_DEV float rq_wp(float4 s)
+{
+    const float ps = __fmul_rn(s.z, 1.0f / 9.0f), qs = __fmul_rn(s.w, 1.0f / 9.0f);
+    return __fmul_rn(qs, rq_rcp(__fadd_rn(__fadd_rn(ps, qs), RCD_EPS)));
+}
+
+/* wt a + (1 - wt) b. */
+CRAW_DEV float rq_blend(float wt, float a, float b)
+{
+    return __fmaf_rn(wt, a, __fmul_rn(__fsub_rn(1.0f, wt), b));
+}
+
+/* Green at an R or B site: its low pass l0, the vertical neighbours vu, vd
+ * (low passes lu, ld two rows away), the horizontal vl, vr (ll, lr), and
+ * the site's vertical weight wt. */
+CRAW_DEV float rq_green(float wt, float l0, float vu, float lu, float vd, float ld, float vl, float ll, float vr,
+                        float lr)
+{
+    const float gv = __fmul_rn(0.5f, __fmaf_rn(vu, rq_ratio1(l0, lu), __fmul_rn(vd, rq_ratio1(l0, ld))));
+    const float gh = __fmul_rn(0.5f, __fmaf_rn(vl, rq_ratio1(l0, ll), __fmul_rn(vr, rq_ratio1(l0, lr))));
+    return rq_blend(wt, gv, gh);
+}
+
+/* g + (a + b) / 2. */
+CRAW_DEV float rq_half_sum(float g, float a, float b)
+{
+    return __fmaf_rn(0.5f, __fadd_rn(a, b), g);
+}
+
+/* The missing colour at an R or B site from the colour differences on its
+ * diagonals (sw + ne against nw + se), by its diagonal weight wt. */
+CRAW_DEV float rq_cross(float wt, float g00, float dsw, float dne, float dnw, float dse)
+{
+    return rq_blend(wt, rq_half_sum(g00, dsw, dne), rq_half_sum(g00, dnw, dse));
+}
+
+/* R and B at a green site: horizontal (dh: the row's colour differences,
+ * ev: the column's of the other colour) against vertical (dv, eh). */
+CRAW_DEV void rq_green_site(float wt, float g00, float dh0, float dh1, float ev0, float ev1, float dv0,
+                            float dv1, float eh0, float eh1, float &ch, float &cv)
+{
+    ch = rq_blend(wt, rq_half_sum(g00, ev0, ev1), rq_half_sum(g00, dh0, dh1));
+    cv = rq_blend(wt, rq_half_sum(g00, dv0, dv1), rq_half_sum(g00, eh0, eh1));
+}
+
 /* ------------------------------------------------------- RCD, by quads */
 
 /* The RCD of an interior tile (all aprons inside the frame), one thread
@@ -406,22 +514,16 @@ struct RcdQuads {
 #pragma unroll
             for (int s = 0; s < 2; s++) {
                 const int cy = 2 + s, cx = 2 + s;
-                lo[s] = (4.0f * v[cy][cx] + 2.0f * (v[cy - 1][cx] + v[cy + 1][cx] + v[cy][cx - 1] + v[cy][cx + 1])
-                         + v[cy - 1][cx - 1] + v[cy - 1][cx + 1] + v[cy + 1][cx - 1] + v[cy + 1][cx + 1]) * (1.0f / 16.0f);
+                lo[s] = rq_lowpass(v[cy][cx], v[cy - 1][cx], v[cy + 1][cx], v[cy][cx - 1], v[cy][cx + 1],
+                                   v[cy - 1][cx - 1], v[cy - 1][cx + 1], v[cy + 1][cx - 1], v[cy + 1][cx + 1]);
             }
             Lat(qx, qy) = make_float2(lo[0], lo[1]);
 #pragma unroll
             for (int b = 0; b < 2; b++)
 #pragma unroll
                 for (int a = 0; a < 2; a++) {
-                    const int cy = 2 + b, cx = 2 + a;
-                    float c2 = 2.0f * v[cy][cx];
-                    float4 d;
-                    d.x = fabsf(v[cy - 1][cx] - v[cy + 1][cx]) + fabsf(c2 - v[cy - 2][cx] - v[cy + 2][cx]);
-                    d.y = fabsf(v[cy][cx - 1] - v[cy][cx + 1]) + fabsf(c2 - v[cy][cx - 2] - v[cy][cx + 2]);
-                    d.z = fabsf(v[cy + 1][cx - 1] - v[cy - 1][cx + 1]) + fabsf(c2 - v[cy + 2][cx - 2] - v[cy - 2][cx + 2]);
-                    d.w = fabsf(v[cy - 1][cx - 1] - v[cy + 1][cx + 1]) + fabsf(c2 - v[cy - 2][cx - 2] - v[cy + 2][cx + 2]);
-                    D(2 * qx + a, 2 * qy + b) = d;
+                    auto win = [&](int r, int c) { return v[b + r][a + c]; };
+                    D(2 * qx + a, 2 * qy + b) = rq_disc4(win);
                 }
         }
         __syncthreads();
@@ -440,32 +542,28 @@ struct RcdQuads {
             for (int r = 0; r < 4; r++) {
                 float4 d0 = D(2 * qx - 1, 2 * qy - 1 + r), d1 = D(2 * qx, 2 * qy - 1 + r);
                 float4 d2 = D(2 * qx + 1, 2 * qy - 1 + r), d3 = D(2 * qx + 2, 2 * qy - 1 + r);
-                float4 mid = make_float4(d1.x + d2.x, d1.y + d2.y, d1.z + d2.z, d1.w + d2.w);
-                h[r][0] = make_float4(d0.x + mid.x, d0.y + mid.y, d0.z + mid.z, d0.w + mid.w);
-                h[r][1] = make_float4(mid.x + d3.x, mid.y + d3.y, mid.z + d3.z, mid.w + d3.w);
+                const float4 mid = rq_add4(d1, d2);
+                h[r][0] = rq_add4(d0, mid);
+                h[r][1] = rq_add4(mid, d3);
             }
 #pragma unroll
             for (int a = 0; a < 2; a++) {
-                float4 mid = make_float4(h[1][a].x + h[2][a].x, h[1][a].y + h[2][a].y,
-                                         h[1][a].z + h[2][a].z, h[1][a].w + h[2][a].w);
+                const float4 mid = rq_add4(h[1][a], h[2][a]);
 #pragma unroll
                 for (int b = 0; b < 2; b++) {
-                    float4 o = b == 0 ? h[0][a] : h[3][a];
-                    float vs = (o.x + mid.x) * (1.0f / 9.0f), hs = (o.y + mid.y) * (1.0f / 9.0f);
-                    float ps = (o.z + mid.z) * (1.0f / 9.0f), qs = (o.w + mid.w) * (1.0f / 9.0f);
-                    wv[b][a] = __fdividef(hs, hs + vs + RCD_EPS);
-                    W(2 * qx + a, 2 * qy + b) = make_float2(wv[b][a], __fdividef(qs, ps + qs + RCD_EPS));
+                    const float4 sum = rq_add4(b == 0 ? h[0][a] : h[3][a], mid);
+                    wv[b][a] = rq_wv(sum);
+                    W(2 * qx + a, 2 * qy + b) = make_float2(wv[b][a], rq_wp(sum));
                 }
             }
             const int x = 2 * qx, y = 2 * qy;
             float2 l0 = Lat(qx, qy), lu = Lat(qx, qy - 1), ld = Lat(qx, qy + 1);
             float2 ll = Lat(qx - 1, qy), lr = Lat(qx + 1, qy);
-            float gv = 0.5f * (V(x, y - 1) * (1.0f + rcd_ratio(l0.x, lu.x)) + V(x, y + 1) * (1.0f + rcd_ratio(l0.x, ld.x)));
-            float gh = 0.5f * (V(x - 1, y) * (1.0f + rcd_ratio(l0.x, ll.x)) + V(x + 1, y) * (1.0f + rcd_ratio(l0.x, lr.x)));
-            float g_r = wv[0][0] * gv + (1.0f - wv[0][0]) * gh;
-            gv = 0.5f * (V(x + 1, y) * (1.0f + rcd_ratio(l0.y, lu.y)) + V(x + 1, y + 2) * (1.0f + rcd_ratio(l0.y, ld.y)));
-            gh = 0.5f * (V(x, y + 1) * (1.0f + rcd_ratio(l0.y, ll.y)) + V(x + 2, y + 1) * (1.0f + rcd_ratio(l0.y, lr.y)));
-            G(qx, qy) = make_float2(g_r, wv[1][1] * gv + (1.0f - wv[1][1]) * gh);
+            const float g_r = rq_green(wv[0][0], l0.x, V(x, y - 1), lu.x, V(x, y + 1), ld.x, V(x - 1, y), ll.x,
+                                       V(x + 1, y), lr.x);
+            const float g_b = rq_green(wv[1][1], l0.y, V(x + 1, y), lu.y, V(x + 1, y + 2), ld.y, V(x, y + 1), ll.y,
+                                       V(x + 2, y + 1), lr.y);
+            G(qx, qy) = make_float2(g_r, g_b);
         }
         __syncthreads();
         /* The missing colour at R (from the B diagonals) and at B (from the
@@ -478,16 +576,16 @@ struct RcdQuads {
             const int x = 2 * qx, y = 2 * qy;
             float c_r = 0.0f, c_b = 0.0f;
             if (qx >= 0 && qy >= 0) {
-                float g00 = G(qx, qy).x, wt = W(x, y).y;
-                float dsw = V(x - 1, y + 1) - G(qx - 1, qy).y, dne = V(x + 1, y - 1) - G(qx, qy - 1).y;
-                float dnw = V(x - 1, y - 1) - G(qx - 1, qy - 1).y, dse = V(x + 1, y + 1) - G(qx, qy).y;
-                c_r = wt * (g00 + 0.5f * (dsw + dne)) + (1.0f - wt) * (g00 + 0.5f * (dnw + dse));
+                const float g00 = G(qx, qy).x;
+                c_r = rq_cross(W(x, y).y, g00, __fsub_rn(V(x - 1, y + 1), G(qx - 1, qy).y),
+                               __fsub_rn(V(x + 1, y - 1), G(qx, qy - 1).y),
+                               __fsub_rn(V(x - 1, y - 1), G(qx - 1, qy - 1).y), __fsub_rn(V(x + 1, y + 1), G(qx, qy).y));
             }
             if (qx < QW && qy < QH) {
-                float g00 = G(qx, qy).y, wt = W(x + 1, y + 1).y;
-                float dsw = V(x, y + 2) - G(qx, qy + 1).x, dne = V(x + 2, y) - G(qx + 1, qy).x;
-                float dnw = V(x, y) - G(qx, qy).x, dse = V(x + 2, y + 2) - G(qx + 1, qy + 1).x;
-                c_b = wt * (g00 + 0.5f * (dsw + dne)) + (1.0f - wt) * (g00 + 0.5f * (dnw + dse));
+                const float g00 = G(qx, qy).y;
+                c_b = rq_cross(W(x + 1, y + 1).y, g00, __fsub_rn(V(x, y + 2), G(qx, qy + 1).x),
+                               __fsub_rn(V(x + 2, y), G(qx + 1, qy).x), __fsub_rn(V(x, y), G(qx, qy).x),
+                               __fsub_rn(V(x + 2, y + 2), G(qx + 1, qy + 1).x));
             }
             Cat(qx, qy) = make_float2(c_r, c_b);
         }
@@ -507,26 +605,18 @@ struct RcdQuads {
             o[0][0] = top.x; o[0][1] = g0.x; o[0][2] = c0.x;
             /* B */
             o[3][0] = c0.y; o[3][1] = g0.y; o[3][2] = bot.y;
-            {   /* Gr at (x + 1, y) */
-                float g00 = top.y, wt = W(x + 1, y).x;
-                float dh = 0.5f * ((top.x - g0.x) + (V(x + 2, y) - gr.x));
-                float ev = 0.5f * ((cu.y - gu.y) + (c0.y - g0.y));
-                float ch = wt * (g00 + ev) + (1.0f - wt) * (g00 + dh);
-                float dv = 0.5f * ((V(x + 1, y - 1) - gu.y) + (bot.y - g0.y));
-                float eh = 0.5f * ((c0.x - g0.x) + (cr.x - gr.x));
-                float cv = wt * (g00 + dv) + (1.0f - wt) * (g00 + eh);
-                o[1][0] = ch; o[1][1] = g00; o[1][2] = cv;
-            }
-            {   /* Gb at (x, y + 1) */
-                float g00 = bot.x, wt = W(x, y + 1).x;
-                float dh = 0.5f * ((V(x - 1, y + 1) - gl.y) + (bot.y - g0.y));
-                float ev = 0.5f * ((c0.x - g0.x) + (cd.x - gd.x));
-                float ch = wt * (g00 + ev) + (1.0f - wt) * (g00 + dh);
-                float dv = 0.5f * ((top.x - g0.x) + (V(x, y + 2) - gd.x));
-                float eh = 0.5f * ((cl.y - gl.y) + (c0.y - g0.y));
-                float cv = wt * (g00 + dv) + (1.0f - wt) * (g00 + eh);
-                o[2][0] = cv; o[2][1] = g00; o[2][2] = ch;
-            }
+            rq_green_site(W(x + 1, y).x, top.y,
+                          __fsub_rn(top.x, g0.x), __fsub_rn(V(x + 2, y), gr.x),
+                          __fsub_rn(cu.y, gu.y), __fsub_rn(c0.y, g0.y),
+                          __fsub_rn(V(x + 1, y - 1), gu.y), __fsub_rn(bot.y, g0.y),
+                          __fsub_rn(c0.x, g0.x), __fsub_rn(cr.x, gr.x), o[1][0], o[1][2]);
+            o[1][1] = top.y;                                   /* Gr at (x + 1, y) */
+            rq_green_site(W(x, y + 1).x, bot.x,
+                          __fsub_rn(V(x - 1, y + 1), gl.y), __fsub_rn(bot.y, g0.y),
+                          __fsub_rn(c0.x, g0.x), __fsub_rn(cd.x, gd.x),
+                          __fsub_rn(top.x, g0.x), __fsub_rn(V(x, y + 2), gd.x),
+                          __fsub_rn(cl.y, gl.y), __fsub_rn(c0.y, g0.y), o[2][2], o[2][0]);
+            o[2][1] = bot.x;                                   /* Gb at (x, y + 1) */
             /* Pixels (x, y), (x + 1, y), (x, y + 1), (x + 1, y + 1) are quad
              * sites 0, 1, 2, 3. */
 #pragma unroll

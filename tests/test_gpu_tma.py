@@ -25,13 +25,17 @@ def ctx():
 
 
 def both(ctx, m, pp, fp):
+    """The RCD interior by tiles (whatever the output space would pick),
+    with plain loads, then with the TMA copy."""
     out = []
+    mode = L.debug_rcd_strips(0)
     for on in (False, True):
         L.debug_rcd_tma(on)
         with L.Pipeline(ctx, pp) as pipe:
             out.append(develop(pipe, m, fp))
             assert pipe.kernel_errors() == 0
     L.debug_rcd_tma(True)
+    L.debug_rcd_strips(mode)
     return out
 
 
