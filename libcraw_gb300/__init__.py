@@ -347,11 +347,13 @@ def awb_signatures() -> dict:
 
 def lib() -> C.CDLL:
     """Loads ``_lib/libcraw.so`` (built by ``libcraw_gb300.build``); raises if
-    it is missing: there is no fallback implementation."""
+    it is missing: there is no fallback implementation. ``CRAW_LIBRARY``
+    names another build of the same library to load instead (the
+    bounds-checked ``_lib/libcraw_bounds.so``)."""
     global _lib
     if _lib is not None:
         return _lib
-    path = LIB_DIR / "libcraw.so"
+    path = Path(os.environ["CRAW_LIBRARY"]) if os.environ.get("CRAW_LIBRARY") else LIB_DIR / "libcraw.so"
     if not path.exists():
         raise ImportError(f"{path} is missing: run libcraw_gb300.build.build() first")
     L = C.CDLL(str(path))

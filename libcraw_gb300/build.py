@@ -7,6 +7,11 @@ Compiles, in parallel and in tree:
   (``csrc/kernels/*.cu``, nvcc ``-gencode arch=compute_103a,code=sm_103a``),
   linked with the static CUDA runtime. Its exported symbols are the
   ``craw_*`` C ABI declared in ``include/craw/*.h``.
+* ``libcraw_gb300/_lib/libcraw_bounds.so`` -- the same library built with
+  ``-DCRAW_DEBUG_BOUNDS=1``: its kernels check their indices against their
+  buffers and report a bad one (CRAW_K_ERR_BOUNDS) instead of making the
+  access (a stand-in for a memory checker; tests load it in a process of
+  their own through ``CRAW_LIBRARY``).
 * ``libcraw_gb300/_lib/libcraw_synth.so`` -- the seeded synthetic-frame
   generator used by the benchmark and the tests (OpenMP).
 * ``oracle/_build/liboracle.so`` -- the CPU oracle (test infrastructure).
@@ -74,21 +79,27 @@ def _run(cmd: list[str]) -> None:
 def build(verbose: bool = False, with_reference: bool | None = None) -> dict[str, Path]:
     """Builds every library; returns their paths. Raises on a failed step."""
     LIB.mkdir(parents=True, exist_ok=True)
-    OBJ.mkdir(parents=True, exist_ok=True)
     (ORACLE / "_build").mkdir(parents=True, exist_ok=True)
     hdr = _headers(ROOT / "include", CSRC)
 
+    # The product, and the bounds-checked variant (the host objects are the
+    # same; the kernels are compiled again with the checks), in one pool.
+    variants = {"libcraw.so": (OBJ, []), "libcraw_bounds.so": (LIB / "obj_bounds", ["-DCRAW_DEBUG_BOUNDS=1"])}
     jobs: list[tuple[Path, list[str], list[Path]]] = []
-    objs: list[Path] = []
+    objs: dict[str, list[Path]] = {}
+    host: list[Path] = []
     for c in sorted((CSRC / "host").glob("*.c")):
         o = OBJ / (c.stem + ".o")
-        objs.append(o)
+        host.append(o)
         jobs.append((o, ["gcc", *HOST_CFLAGS, "-c", str(c), "-o", str(o)], [c]))
-    for cu in sorted((CSRC / "kernels").glob("*.cu")):
-        o = OBJ / (cu.stem + ".cu.o")
-        objs.append(o)
-        jobs.append((o, [NVCC, *NVCC_FLAGS, *NVCC_FILE_FLAGS.get(cu.stem, []), "-c", str(cu), "-o", str(o)],
-                     [cu]))
+    for name, (odir, extra) in variants.items():
+        odir.mkdir(parents=True, exist_ok=True)
+        objs[name] = list(host)
+        for cu in sorted((CSRC / "kernels").glob("*.cu")):
+            o = odir / (cu.stem + ".cu.o")
+            objs[name].append(o)
+            jobs.append((o, [NVCC, *NVCC_FLAGS, *extra, *NVCC_FILE_FLAGS.get(cu.stem, []), "-c", str(cu),
+                             "-o", str(o)], [cu]))
 
     todo = [j for j in jobs if _stale(j[0], j[2], hdr)]
     workers = max(1, min(len(todo), os.cpu_count() or 4))
@@ -99,10 +110,12 @@ def build(verbose: bool = False, with_reference: bool | None = None) -> dict[str
         if verbose:
             print(f"compiled {len(todo)} objects", file=sys.stderr)
 
+    for name in variants:
+        so = LIB / name
+        if _stale(so, objs[name], 0.0):
+            _run([NVCC, "-shared", *ARCH, "-cudart", "static", "-o", str(so), *map(str, objs[name]),
+                  "-Xlinker", "--exclude-libs,ALL", "-lm"])
     so = LIB / "libcraw.so"
-    if _stale(so, objs, 0.0):
-        _run([NVCC, "-shared", *ARCH, "-cudart", "static", "-o", str(so), *map(str, objs),
-              "-Xlinker", "--exclude-libs,ALL", "-lm"])
 
     synth_src = CSRC / "synth" / "synth.c"
     synth = LIB / "libcraw_synth.so"
@@ -120,7 +133,7 @@ def build(verbose: bool = False, with_reference: bool | None = None) -> dict[str
               "-fvisibility=hidden", f"-I{ROOT / 'include'}", f"-I{CUDA_HOME / 'include'}",
               str(orc_src), "-o", str(orc), "-lm"])
 
-    out = {"craw": so, "synth": synth, "oracle": orc}
+    out = {"craw": so, "craw_bounds": LIB / "libcraw_bounds.so", "synth": synth, "oracle": orc}
     if with_reference is None:
         with_reference = (REFERENCE / "lib" / "ref").is_dir()
     if with_reference and shutil.which("gcc"):

@@ -203,8 +203,10 @@ typedef struct CRAWKDevelopIO {
 } CRAWKDevelopIO;
 
 /* Kernel error bits: a wait on a TMA copy that did not complete within
- * its bound (the tile is skipped). */
+ * its bound (the tile is skipped); an index outside its buffer, found by
+ * the checks of a CRAW_DEBUG_BOUNDS build (the access is skipped). */
 #define CRAW_K_ERR_TMA_WAIT 1u
+#define CRAW_K_ERR_BOUNDS 2u
 
 /* Prep + debayer + (colour to dst | chroma block means) + AWB records +
  * optional intermediate, in one kernel. */

@@ -13,6 +13,26 @@
 
 #define CRAW_DEV __device__ __forceinline__
 
+/* Index checks of the CRAW_DEBUG_BOUNDS build (the library built with
+ * -DCRAW_DEBUG_BOUNDS=1 as _lib/libcraw_bounds.so): `ok` is the check of
+ * an index against its buffer; a failed one sets CRAW_K_ERR_BOUNDS in the
+ * kernel's error word `err` (when there is one) and the caller skips the
+ * access, so that no fault, trap or hang follows. In the product build
+ * the check is true and costs nothing. */
+#if defined(CRAW_DEBUG_BOUNDS) && CRAW_DEBUG_BOUNDS
+CRAW_DEV bool craw_in_bounds(bool ok, uint32_t *err)
+{
+    if (!ok && err)
+        atomicOr(err, CRAW_K_ERR_BOUNDS);
+    return ok;
+}
+#else
+CRAW_DEV constexpr bool craw_in_bounds(bool, uint32_t *)
+{
+    return true;
+}
+#endif
+
 /* 0, or -5 (EIO) when a CUDA error of an earlier call is pending on this
  * thread: it is the caller's to read, not ours to clear, and a launch now
  * could not tell its own error from it. Every launcher checks this first,

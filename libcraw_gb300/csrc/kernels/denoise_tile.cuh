@@ -62,11 +62,15 @@ CRAW_DEV float level(const CRAWKDenoise &k, uint32_t raw, int pl)
 /* The four plane samples of mosaic quad (qx, qy): R, Gr, Gb, B. */
 /* The quad at plane position (qx, qy): its two mosaic rows as 32-bit
  * pairs (a: R, Gr; b: Gb, B) and the four samples. */
-CRAW_DEV void load_quad_u16(const CRAWKDenoiseIO &io, int qx, int qy, uint32_t q[4], uint32_t &a, uint32_t &b)
+CRAW_DEV void load_quad_u16(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int qx, int qy, uint32_t q[4],
+                           uint32_t &a, uint32_t &b, uint32_t *err)
 {
-    const char *r0 = (const char *)io.src + (size_t)(2 * qy) * io.src_pitch;
-    a = __ldg(reinterpret_cast<const uint32_t *>(r0) + qx);
-    b = __ldg(reinterpret_cast<const uint32_t *>(r0 + io.src_pitch) + qx);
+    a = b = 0u;
+    if (craw_in_bounds(qx >= 0 && qx < k.pw && qy >= 0 && qy < k.ph, err)) {
+        const char *r0 = (const char *)io.src + (size_t)(2 * qy) * io.src_pitch;
+        a = __ldg(reinterpret_cast<const uint32_t *>(r0) + qx);
+        b = __ldg(reinterpret_cast<const uint32_t *>(r0 + io.src_pitch) + qx);
+    }
     q[0] = a & 0xffffu; q[1] = a >> 16; q[2] = b & 0xffffu; q[3] = b >> 16;
 }
 
@@ -81,11 +85,15 @@ CRAW_DEV void keep_raw(uint32_t *rw, int cr, int cc, uint32_t a, uint32_t b)
     }
 }
 
-CRAW_DEV void load_quad_f32(const float *base, size_t pitch, int qx, int qy, float q[4])
+CRAW_DEV void load_quad_f32(const CRAWKDenoise &k, const float *base, size_t pitch, int qx, int qy, float q[4],
+                           uint32_t *err)
 {
-    const char *r0 = (const char *)base + (size_t)(2 * qy) * pitch;
-    float2 a = __ldg(reinterpret_cast<const float2 *>(r0) + qx);
-    float2 b = __ldg(reinterpret_cast<const float2 *>(r0 + pitch) + qx);
+    float2 a = make_float2(0.f, 0.f), b = a;
+    if (craw_in_bounds(qx >= 0 && qx < k.pw && qy >= 0 && qy < k.ph, err)) {
+        const char *r0 = (const char *)base + (size_t)(2 * qy) * pitch;
+        a = __ldg(reinterpret_cast<const float2 *>(r0) + qx);
+        b = __ldg(reinterpret_cast<const float2 *>(r0 + pitch) + qx);
+    }
     q[0] = a.x; q[1] = a.y; q[2] = b.x; q[3] = b.y;
 }
 
@@ -449,7 +457,7 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
                 q[0] = qa & 0xffffu; q[1] = qa >> 16; q[2] = qb & 0xffffu; q[3] = qb >> 16;
             } else {
                 int qy = craw_mirror(ty0 - R + r, k.ph), qx = craw_mirror(tx0 - R + c, k.pw);
-                load_quad_u16(io, qx, qy, q, qa, qb);
+                load_quad_u16(k, io, qx, qy, q, qa, qb, err);
             }
             if constexpr (STAGED)
                 keep_raw<OX, OY>(raw32, r - R, c - R, qa, qb);
@@ -468,10 +476,10 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
             int qy = craw_mirror(ty0 - R - 1 + r, k.ph), qx = craw_mirror(tx0 - R - 1 + c, k.pw);
             uint32_t q[4], qa, qb;
             float lp[4];
-            load_quad_u16(io, qx, qy, q, qa, qb);
+            load_quad_u16(k, io, qx, qy, q, qa, qb, err);
             if constexpr (STAGED)
                 keep_raw<OX, OY>(raw32, r - R - 1, c - R - 1, qa, qb);
-            load_quad_f32(io.lvl_prev, io.lvl_pitch, qx, qy, lp);
+            load_quad_f32(k, io.lvl_prev, io.lvl_pitch, qx, qy, lp, err);
 #pragma unroll
             for (int pl = 0; pl < 4; pl++) {
                 TC[pl * C::EN + i] = gat_fwd(k, level(k, q[pl], pl));
@@ -493,8 +501,11 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
             for (int j = 0; j < KR; j++) {
                 const int qy = craw_mirror(ty0 - R + r0 + j, k.ph);
                 const char *vr = (const char *)io.var_prev + (size_t)(2 * qy) * io.var_pitch;
-                const uint16_t v0 = __ldg(reinterpret_cast<const uint16_t *>(vr) + qx);
-                const uint16_t v1 = __ldg(reinterpret_cast<const uint16_t *>(vr + io.var_pitch) + qx);
+                uint16_t v0 = 0, v1 = 0;
+                if (craw_in_bounds(qx >= 0 && qx < k.pw && qy >= 0 && qy < k.ph, err)) {
+                    v0 = __ldg(reinterpret_cast<const uint16_t *>(vr) + qx);
+                    v1 = __ldg(reinterpret_cast<const uint16_t *>(vr + io.var_pitch) + qx);
+                }
                 sv[j][0] = v0 & 0xffu;
                 sv[j][1] = (uint32_t)v0 >> 8;
                 sv[j][2] = v1 & 0xffu;
@@ -593,7 +604,7 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
         for (int j = 0; j < BW; j++) {
             const int qx = tx0 + ox0 + j;
             near[j] = false;
-            if (qy >= k.ph || qx >= k.pw)
+            if (qy >= k.ph || qx >= k.pw || !craw_in_bounds(qx >= 0 && qy >= 0, err))
                 continue;
             const int my = 2 * qy + py, mx = 2 * qx + px;
             const float tc = Tp[(oy0 + R + m) * TS + ox0 + R + j];
@@ -643,8 +654,10 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
                 const uint32_t b1 = __ballot_sync(0xffffffffu, near[1]);
                 const uint32_t sh = lane & 16;
                 const uint32_t word = ((b0 >> sh) & 0xffffu) | (((b1 >> sh) & 0xffffu) << 16);
-                if ((lane & 15) == 0 && qy < k.ph)
-                    rd->flags[((size_t)pl * k.ph + qy) * CRAW_K_ROUND_WW(k.pw) + (tx0 >> 5)] = word;
+                const size_t wi = ((size_t)pl * k.ph + qy) * CRAW_K_ROUND_WW(k.pw) + (tx0 >> 5);
+                if ((lane & 15) == 0 && qy < k.ph &&
+                    craw_in_bounds(wi < (size_t)CRAW_K_ROUND_WORDS(k.pw, k.ph), err))
+                    rd->flags[wi] = word;
             }
         }
     }
@@ -660,7 +673,7 @@ CRAW_DEV void denoise_tile(const CRAWKDenoise &k, const CRAWKDenoiseIO &io, int 
     const uint16_t *raw16 = reinterpret_cast<const uint16_t *>(raw32);
     for (int i = tid; i < C::RW_H * CH; i += NT) {
         const int yy = i / CH, xx = (i % CH) * 8, my = my0 + yy, mx = mx0 + xx;
-        if (my >= H || mx >= W)
+        if (my >= H || mx >= W || !craw_in_bounds(my >= 0 && mx >= 0 && yy < C::RW_H, err))
             continue;
         uint16_t *dr = (uint16_t *)((char *)io.dst + (size_t)my * io.dst_pitch) + mx;
         if (a16 && mx + 8 <= W) {

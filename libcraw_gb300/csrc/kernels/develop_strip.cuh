@@ -88,7 +88,10 @@ struct Strip {
      * pixel row yr, as its two raw samples. */
     CRAW_DEV uint32_t fetch(int yr, int m) const
     {
-        const char *row = (const char *)io.src + (size_t)(2 * oy + yr) * io.src_pitch;
+        const int y = 2 * oy + yr, x = 2 * (ox - 3 + m);
+        if (!craw_in_bounds(y >= 0 && y < k.height && x >= 0 && x + 1 < k.width, io.err))
+            return 0u;
+        const char *row = (const char *)io.src + (size_t)y * io.src_pitch;
         return __ldg(reinterpret_cast<const uint32_t *>(row) + (ox - 3 + m));
     }
     CRAW_DEV void put(int yr, int m, uint32_t raw) const
@@ -100,7 +103,8 @@ struct Strip {
             const int s0 = (yr & 1) * 2;
             t = make_float2(craw_prep(k, (uint16_t)(raw & 0xffff), s0), craw_prep(k, (uint16_t)(raw >> 16), s0 + 1));
         }
-        *reinterpret_cast<float2 *>(&S.v[(yr & (SVR - 1)) * SVS + 2 * m]) = t;
+        if (craw_in_bounds(m >= 0 && 2 * m + 1 < SVS, io.err))
+            *reinterpret_cast<float2 *>(&S.v[(yr & (SVR - 1)) * SVS + 2 * m]) = t;
     }
 };
 
@@ -170,9 +174,11 @@ CRAW_DEV void rcd_strip(const CRAWKDevelop &k, const CRAWKDevelopIO &io, const S
             const float sg = __shfl_down_sync(0xffffffffu, asum, 1), sb = __shfl_down_sync(0xffffffffu, asum, 2);
             if (folder && ac == 0) {
                 const int bx = (2 * t.ox) / 8 + ab, by = (2 * t.oy + 2 * r - 6) / 8;
-                io.awb.rec[(size_t)by * ((k.width + 7) / 8) + bx] =
-                    craw_awb_block(__fdiv_rn(asum, 64.0f), __fdiv_rn(sg, 64.0f), __fdiv_rn(sb, 64.0f), k.awb_wb,
-                                   io.awb.deferred, io.awb.nb_deferred, craw_awb_blocks(k.width, k.height));
+                const size_t ri = (size_t)by * ((k.width + 7) / 8) + bx;
+                if (craw_in_bounds(bx >= 0 && by >= 0 && ri < craw_awb_blocks(k.width, k.height), io.err))
+                    io.awb.rec[ri] = craw_awb_block(__fdiv_rn(asum, 64.0f), __fdiv_rn(sg, 64.0f),
+                                                    __fdiv_rn(sb, 64.0f), k.awb_wb, io.awb.deferred,
+                                                    io.awb.nb_deferred, craw_awb_blocks(k.width, k.height));
             }
             asum = 0.0f;
         }
@@ -189,6 +195,8 @@ CRAW_DEV void rcd_strip(const CRAWKDevelop &k, const CRAWKDevelopIO &io, const S
             const int jj = i >= rw, c = i - jj * rw;
             const float v[3] = { S.a[0][jj][c], S.a[1][jj][c], S.a[2][jj][c] };
             const int px = 2 * t.ox + c, py = 2 * (t.oy + r) + jj;
+            if (!craw_in_bounds(px >= 0 && px < k.width && py >= 0 && py < k.height && c < SAW, io.err))
+                continue;
             if (io.inter)
                 craw_store_rgba(io.inter, io.inter_pitch, px, py, k.fp16, v[0], v[1], v[2]);
             if (io.dst) {

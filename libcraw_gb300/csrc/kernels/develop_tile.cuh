@@ -73,7 +73,9 @@ CRAW_DEV void load_prepped(const CRAWKDevelop &k, const CRAWKDevelopIO &io, cons
             x = craw_mirror(x, f.w);
             y = craw_mirror(y, f.h);
         }
-        uint16_t raw = __ldg((const uint16_t *)((const char *)io.src + (size_t)y * io.src_pitch) + x);
+        uint16_t raw = 0;
+        if (craw_in_bounds(x >= 0 && x < k.width && y >= 0 && y < k.height, io.err))
+            raw = __ldg((const uint16_t *)((const char *)io.src + (size_t)y * io.src_pitch) + x);
         v.p[i] = io.src_f16 ? __half2float(__ushort_as_half(raw)) : craw_prep(k, raw, (y & 1) * 2 + (x & 1));
     }
 }
@@ -469,8 +471,11 @@ struct RcdQuads {
             qy -= 3;
             int x = x0 + 2 * qx, y = y0 + 2 * qy;
             const char *r0 = (const char *)io.src + (size_t)y * io.src_pitch;
-            uint32_t a = __ldg(reinterpret_cast<const uint32_t *>(r0) + x / 2);
-            uint32_t b = __ldg(reinterpret_cast<const uint32_t *>(r0 + io.src_pitch) + x / 2);
+            uint32_t a = 0, b = 0;
+            if (craw_in_bounds(x >= 0 && x + 1 < k.width && y >= 0 && y + 1 < k.height, io.err)) {
+                a = __ldg(reinterpret_cast<const uint32_t *>(r0) + x / 2);
+                b = __ldg(reinterpret_cast<const uint32_t *>(r0 + io.src_pitch) + x / 2);
+            }
             put_quad(k, io, qx, qy, a, b);
         }
     }
@@ -664,7 +669,7 @@ CRAW_DEV void epilogue(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, 
                 rgb[c * P + i] = v[c];
             }
         }
-        if (x >= k.width || y >= k.height)
+        if (x >= k.width || y >= k.height || !craw_in_bounds(x >= 0 && y >= 0, io.err))
             continue;
         if (io.inter)
             craw_store_rgba(io.inter, io.inter_pitch, x, y, k.fp16, v[0], v[1], v[2]);
@@ -757,7 +762,10 @@ CRAW_DEV void awb_blocks(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0
                 }
         }
         float n = (float)(xe * ye);
-        io.awb.rec[(size_t)(y0 / 8 + by) * blocks_x + x0 / 8 + bx] =
+        const size_t ri = (size_t)(y0 / 8 + by) * blocks_x + x0 / 8 + bx;
+        if (!craw_in_bounds(ri < craw_awb_blocks(k.width, k.height), io.err))
+            continue;
+        io.awb.rec[ri] =
             craw_awb_block(__fdiv_rn(s0, n), __fdiv_rn(s1, n), __fdiv_rn(s2, n), k.awb_wb,
                            io.awb.deferred, io.awb.nb_deferred,
                            craw_awb_blocks(k.width, k.height));
