@@ -39,7 +39,10 @@ typedef struct CRAWServerParams {
     uint32_t max_inflight;         /* frames on the device at once; 0: 32 */
     uint32_t slots_per_stream;     /* staging slots (frames in flight) per stream; 0: 2 */
     uint32_t idle_timeout_ms;      /* 0: streams are only closed by their owner */
-    uint8_t padding[64 - 20];
+    uint32_t max_queued;           /* frames a stream may have waiting for the device;
+                                    * a submit beyond it returns EAGAIN at once (the
+                                    * producer polls and submits again); 0: no limit */
+    uint8_t padding[64 - 24];
 } CRAWServerParams;
 
 /* Stream flags. */
@@ -66,7 +69,11 @@ typedef struct CRAWServerStreamParams {
     uint32_t flags;                /* CRAW_SERVER_STREAM_* */
     CRAWAwbParams awb;             /* estimator, with AUTO_WB */
     CRAWAwbSmootherParams smoother;
-    uint8_t padding[64];
+    float deadline_ms;             /* the latency a frame of the stream should meet (its
+                                    * frame interval, say): waiting frames launch earliest
+                                    * deadline first; 0: none (best effort, after every
+                                    * stream with one) */
+    uint8_t padding[60];
 } CRAWServerStreamParams;
 
 typedef struct CRAWServerResult {
@@ -88,6 +95,7 @@ typedef struct CRAWServerStats {
     uint32_t streams, queued, inflight;
     uint64_t submitted, completed, failed;
     uint64_t streams_admitted, streams_refused, streams_reclaimed;
+    uint64_t submits_refused;            /* EAGAIN: the stream's queue was full */
 } CRAWServerStats;
 
 CRAW_API void craw_server_params_init(CRAWServerParams *p);
@@ -117,7 +125,9 @@ CRAW_API int craw_server_stream_close(CRAWServer *s, uint32_t stream_id);
  * output format; both must stay valid until the frame's result is polled.
  * `fp` is copied (its profile must outlive the frame). `pts` is the
  * presentation time in seconds (AWB track). Returns at once;
- * CRAW_ERROR(ENOENT) for a stream that is not open. */
+ * CRAW_ERROR(ENOENT) for a stream that is not open, CRAW_ERROR(EAGAIN)
+ * when the stream already has max_queued frames waiting (nothing is
+ * queued: poll for results and submit again). */
 CRAW_API int craw_server_submit(CRAWServer *s, uint32_t stream_id, const void *src,
                                 size_t src_pitch, void *dst, size_t dst_pitch,
                                 const CRAWFrameParams *fp, double pts, uint64_t user);

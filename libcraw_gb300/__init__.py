@@ -224,12 +224,12 @@ class AwbSmootherParams(C.Structure):
 class ServerParams(C.Structure):
     _fields_ = [("hbm_budget", C.c_uint64), ("max_inflight", C.c_uint32),
                 ("slots_per_stream", C.c_uint32), ("idle_timeout_ms", C.c_uint32),
-                ("padding", C.c_uint8 * 44)]
+                ("max_queued", C.c_uint32), ("padding", C.c_uint8 * 40)]
 
 
 class ServerStreamParams(C.Structure):
     _fields_ = [("pipeline", PipelineParams), ("flags", C.c_uint32), ("awb", AwbParams),
-                ("smoother", AwbSmootherParams), ("padding", C.c_uint8 * 64)]
+                ("smoother", AwbSmootherParams), ("deadline_ms", C.c_float), ("padding", C.c_uint8 * 60)]
 
 
 class ServerResult(C.Structure):
@@ -243,7 +243,8 @@ class ServerStats(C.Structure):
     _fields_ = [("hbm_budget", C.c_uint64), ("hbm_resident", C.c_uint64), ("streams", C.c_uint32),
                 ("queued", C.c_uint32), ("inflight", C.c_uint32), ("submitted", C.c_uint64),
                 ("completed", C.c_uint64), ("failed", C.c_uint64), ("streams_admitted", C.c_uint64),
-                ("streams_refused", C.c_uint64), ("streams_reclaimed", C.c_uint64)]
+                ("streams_refused", C.c_uint64), ("streams_reclaimed", C.c_uint64),
+                ("submits_refused", C.c_uint64)]
 
 
 SERVER_STREAM_AUTO_WB = 1 << 0
@@ -773,11 +774,13 @@ def server_params(**kw) -> ServerParams:
     return p
 
 
-def server_stream_params(pipeline: PipelineParams, flags: int = 0) -> ServerStreamParams:
+def server_stream_params(pipeline: PipelineParams, flags: int = 0,
+                         deadline_ms: float = 0.0) -> ServerStreamParams:
     p = ServerStreamParams()
     lib().craw_server_stream_params_init(C.byref(p))
     p.pipeline = pipeline
     p.flags = flags
+    p.deadline_ms = deadline_ms
     return p
 
 

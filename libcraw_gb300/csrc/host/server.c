@@ -1,9 +1,10 @@
 /*
  * The frame server (include/craw/server.h): streams admitted against a
  * device-memory budget, a queue of frames, and one worker thread that
- * keeps the device busy with every frame that has a free slot, retires
- * finished frames by polling their events, and runs the AWB loop of the
- * streams that keep a track.
+ * keeps the device busy with every frame that has a free slot (earliest
+ * deadline first), retires finished frames by polling their events, and runs
+ * the AWB loop of the streams that keep a track. A stream's waiting
+ * frames are bounded by max_queued: beyond it a submit returns EAGAIN.
  *
  * Locking: one mutex guards everything the worker and the callers share.
  * The worker drops it only around the AWB estimate (host work of a few
@@ -38,7 +39,8 @@ struct job {
     double pts;
     uint64_t user;
     uint64_t seq;                    /* submission order within the server */
-    double t_submit, t_launch;
+    int sidx;                        /* its stream's index in streams[] */
+    double t_submit, t_launch, due;  /* due: t_submit + the stream's deadline */
     bool noise_measured;             /* the stream's noise model came from this frame */
 };
 
@@ -236,63 +238,64 @@ static int launch(CRAWServer *s, struct stream *st, struct slot *sl, struct job 
     return 0;
 }
 
-/* Starts every queued frame that may start (lock held): the first queued
- * frame of each stream, when the stream has a free slot (and, keeping an
- * AWB track, nothing in flight) and the device has room. */
+/* Starts every queued frame that may start (lock held): of the first
+ * queued frame of each stream whose stream has a free slot (and, keeping
+ * an AWB track, nothing in flight), the one due first, while the device
+ * has room; a stream's own frames start in their order. */
 static bool launch_ready(CRAWServer *s)
 {
-    bool blocked[MAX_STREAMS] = { false };
-    struct job **pj = &s->q_head, *prev = NULL;
     bool progress = false;
 
-    while (*pj && s->stats.inflight < s->params.max_inflight) {
-        struct job *j = *pj;
-        struct stream *st = find_stream(s, j->stream);
-        int si = -1, idx = -1;
+    while (s->stats.inflight < s->params.max_inflight) {
+        bool seen[MAX_STREAMS] = { false };
+        struct job *best = NULL, *best_prev = NULL, *prev = NULL;
+        int best_slot = -1;
 
-        for (int i = 0; st && i < MAX_STREAMS; i++)
-            if (s->streams[i] == st)
-                idx = i;
-        if (st && !blocked[idx] && !st->busy_host &&
-            !((st->params.flags & CRAW_SERVER_STREAM_AUTO_WB) && st->inflight)) {
-            for (uint32_t k = 0; k < st->nb_slots; k++)
-                if (!st->slots[k].job) {
+        for (struct job *j = s->q_head; j; prev = j, j = j->next) {
+            struct stream *st = s->streams[j->sidx];
+            int si = -1;
+            if (seen[j->sidx])
+                continue;
+            seen[j->sidx] = true;
+            if (!st || st->id != j->stream || st->busy_host ||
+                ((st->params.flags & CRAW_SERVER_STREAM_AUTO_WB) && st->inflight))
+                continue;
+            for (uint32_t k = 0; k < st->nb_slots && si < 0; k++)
+                if (!st->slots[k].job)
                     si = (int)k;
-                    break;
-                }
+            if (si >= 0 && (!best || j->due < best->due)) {
+                best = j;
+                best_prev = prev;
+                best_slot = si;
+            }
         }
-        if (st && si < 0) {
-            blocked[idx] = true;     /* later frames of this stream wait too */
-            prev = j;
-            pj = &j->next;
-            continue;
-        }
+        if (!best)
+            break;
         /* Unlink. */
-        *pj = j->next;
-        if (s->q_tail == j)
-            s->q_tail = prev;
+        if (best_prev)
+            best_prev->next = best->next;
+        else
+            s->q_head = best->next;
+        if (s->q_tail == best)
+            s->q_tail = best_prev;
         s->stats.queued--;
         progress = true;
-        j->t_launch = now_ms();
-        if (!st) {                   /* the stream went away: cannot happen while queued */
-            fail_job(s, j, CRAW_ERROR(ENOENT), j->t_launch);
-            free(j);
-            continue;
-        }
-        st->queued--;
+        best->t_launch = now_ms();
         {
-            struct slot *sl = &st->slots[si];
-            int ret = launch(s, st, sl, j);
-            if (ret < 0) {
+            struct stream *st = s->streams[best->sidx];
+            struct slot *sl = &st->slots[best_slot];
+            int ret;
+            st->queued--;
+            if ((ret = launch(s, st, sl, best)) < 0) {
                 /* Anything already enqueued for it only touches the slot,
                  * whose next use is ordered after it on the same stream. */
-                fail_job(s, j, ret, now_ms());
-                free(j);
+                fail_job(s, best, ret, now_ms());
+                free(best);
                 st->last_activity = now_ms();
                 pthread_cond_broadcast(&s->idle_cv);
                 continue;
             }
-            sl->job = j;
+            sl->job = best;
             st->inflight++;
             s->stats.inflight++;
         }
@@ -552,6 +555,9 @@ CRAW_API int craw_server_stream_open(CRAWServer *s, const CRAWServerStreamParams
     before = pool_used(s);
     if ((ret = craw_pipeline_create(s->ctx, pp, &st->pipe)) < 0)
         goto fail;
+    /* One stream priority for all: priorities by deadline (tried) starve
+     * the large frames' kernels behind the small ones' and lengthen the
+     * tail of the mix; the deadlines order the launches instead. */
     if (cudaStreamCreateWithFlags(&st->cs, cudaStreamNonBlocking) != cudaSuccess) {
         ret = CRAW_ERROR(ENOMEM);
         goto fail;
@@ -659,7 +665,17 @@ CRAW_API int craw_server_submit(CRAWServer *s, uint32_t id, const void *src, siz
         free(j);
         return CRAW_ERROR(EINVAL);
     }
+    if (s->params.max_queued && st->queued >= s->params.max_queued) {
+        s->stats.submits_refused++;
+        pthread_mutex_unlock(&s->lock);
+        free(j);
+        return CRAW_ERROR(EAGAIN);
+    }
+    for (int i = 0; i < MAX_STREAMS; i++)
+        if (s->streams[i] == st)
+            j->sidx = i;
     j->t_submit = now_ms();
+    j->due = j->t_submit + (st->params.deadline_ms > 0.0f ? (double)st->params.deadline_ms : 1e12);
     j->seq = s->stats.submitted;
     if (s->q_tail)
         s->q_tail->next = j;

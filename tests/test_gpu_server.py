@@ -1,7 +1,8 @@
 """GPU: the frame server (craw_server_*): a stream's results are the same
-alone and in a mix of streams of other sizes (bit for bit, and the same as
-craw_pipeline_record() driven directly), admission under the device-memory
-budget, a dead producer's stream reclaimed, and the closed AWB loop."""
+alone and in a mix of streams of other sizes and deadlines (bit for bit,
+and the same as craw_pipeline_record() driven directly), backpressure on
+submit, admission under the device-memory budget, a dead producer's
+stream reclaimed, and the closed AWB loop."""
 import errno
 import threading
 import time
@@ -89,15 +90,16 @@ def test_same_alone_and_in_the_mix(ctx):
         assert len(res) == len(ms) and all(r.status == 0 for r in res)
         alone = [d.numpy().copy() for d in a.dst]
     # In the mix: three other streams of other sizes and settings, their
-    # frames interleaved with ours and submitted while ours are in flight.
-    others = [(512, 288, 601, True), (96, 64, 602, True), (640, 352, 603, False)]
+    # frames interleaved with ours and submitted while ours are in flight;
+    # the streams have deadlines (earliest-deadline-first launches) or none.
+    others = [(512, 288, 601, True, 33.3), (96, 64, 602, True, 0.0), (640, 352, 603, False, 41.7)]
     with L.Server(ctx, L.server_params(hbm_budget=4 << 30, max_inflight=8)) as srv:
         b = Feed(ms)
-        sid = srv.open(L.server_stream_params(pp))
+        sid = srv.open(L.server_stream_params(pp, deadline_ms=16.7))
         feeds = []
-        for w, h, seed, temporal in others:
+        for w, h, seed, temporal, dl in others:
             f = Feed(frames(w, h, seed, 6))
-            feeds.append((srv.open(L.server_stream_params(pipeline_params(w, h, temporal))), f,
+            feeds.append((srv.open(L.server_stream_params(pipeline_params(w, h, temporal), deadline_ms=dl)), f,
                           fparams(prof, temporal)))
         for i in range(len(ms)):
             for osid, f, ofp in feeds:
@@ -122,6 +124,47 @@ def test_same_alone_and_in_the_mix(ctx):
         assert np.array_equal(x, y), (i, np.nanmax(np.abs(x - y)))
     # And both are craw_pipeline_record's own results.
     for i, (x, y) in enumerate(zip(alone, direct(ctx, ms, pp, fp))):
+        assert np.array_equal(x, y), i
+
+
+def test_backpressure(ctx):
+    """With max_queued, a stream's waiting frames stay bounded: a submit
+    beyond the bound returns EAGAIN at once and queues nothing; the
+    producer polls and submits the same frame again, and the results are
+    the sequence's own, in order."""
+    prof = W.make_profile()
+    fp = fparams(prof)
+    w, h = 5760, 3240
+    ms = frames(w, h, 701, 4)
+    pp = pipeline_params(w, h)
+    with L.Server(ctx, L.server_params(hbm_budget=8 << 30, max_inflight=1, slots_per_stream=1,
+                                       max_queued=1)) as srv:
+        f = Feed(ms)
+        sid = srv.open(L.server_stream_params(pp, deadline_ms=41.7))
+        refused, res = 0, []
+        for i in range(len(ms)):
+            while True:
+                try:
+                    f.submit(srv, sid, i, fp)
+                    break
+                except L.CrawError as e:
+                    assert e.errno == errno.EAGAIN
+                    refused += 1
+                    assert srv.stats().queued <= 1
+                    res += srv.poll(8, 1)
+            assert srv.stats().queued <= 1
+        srv.drain()
+        while True:
+            got = srv.poll(8)
+            if not got:
+                break
+            res += got
+        st = srv.stats()
+        assert refused > 0 and st.submits_refused == refused
+        assert st.completed == len(ms) and st.failed == 0
+        assert [r.user & 0xFFFFFFFF for r in res] == list(range(len(ms)))
+        got_frames = [d.numpy().copy() for d in f.dst]
+    for i, (x, y) in enumerate(zip(got_frames, direct(ctx, ms, pp, fp))):
         assert np.array_equal(x, y), i
 
 
