@@ -77,8 +77,13 @@ def parse():
                     help="denoise tile shape index instead of the autotuner's (profiling)")
     ap.add_argument("--e2e-lanes", type=int, default=0,
                     help="pipelines the end-to-end leg rotates over (0: the default)")
-    ap.add_argument("--width", type=int, default=5760)
-    ap.add_argument("--height", type=int, default=3240)
+    ap.add_argument("--width", type=int, default=None, help="frame width (default: the workload's)")
+    ap.add_argument("--height", type=int, default=None, help="frame height (default: the workload's)")
+    ap.add_argument("--workload", default="nlm_rcd_ap1",
+                    choices=["nlm_rcd_ap1", "batch_rcd_bt2020", "bilinear_bt709_1080p"],
+                    help="the timed single-frame workload: the headline (5760x3240 VST + NLM + RCD + "
+                         "ACES AP1 with the gamut compression), one frame of the batch (the same with "
+                         "BT.2020 output), or 1920x1080 bilinear BT.709; for profiling runs")
     return ap.parse_args()
 
 
@@ -325,8 +330,9 @@ def run_gpu(args):
     dev = torch.cuda.current_device()
     props = torch.cuda.get_device_properties(dev)
 
-    c = W.workload("nlm_rcd_ap1", args.width, args.height)
+    c = W.workload(args.workload, args.width, args.height)
     w, h = c.width, c.height
+    label = WORKLOAD if args.workload == "nlm_rcd_ap1" and (w, h) == (5760, 3240) else f"{w}x{h} {c.name}"
     prof = W.make_profile()
     fp = L.frame_params(prof, **c.frame_kwargs())
     storage = L.STORAGE_FP16 if args.storage == "fp16" else L.STORAGE_FP32
@@ -539,7 +545,7 @@ def run_gpu(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic: seeded generator (gradient + 256 rectangles + 4 zone plates, "
                     "Poisson-Gaussian noise a=4 DN, b=40 DN^2), 4 frames in rotation",
-            "config": {"workload": WORKLOAD, "width": w, "height": h, "impl": args.impl,
+            "config": {"workload": label, "width": w, "height": h, "impl": args.impl,
                        "storage": args.storage, "l2": "flushed between steps (256 MB write)",
                        "rounding": ("exact: denoised codes as an FP64 evaluation rounds them"
                                     if exact else "float (the reference's)"),
