@@ -40,8 +40,10 @@ struct CRAWPipeline;
 
 /* Waits for the pipeline's recordings to finish and returns the error
  * bits its kernels set (1: a TMA copy was not complete within its wait
- * bound; the tile was skipped), clearing them. 0 when all is well; a
- * negative errno if the read fails. */
+ * bound, the tile was skipped; 2: in the bounds-checked build,
+ * libcraw_bounds.so, an index lay outside its buffer, the access was
+ * skipped), clearing them. 0 when all is well; a negative errno if the
+ * read fails. */
 CRAW_API int craw_debug_kernel_errors(struct CRAWPipeline *pipe);
 
 /* The exact rounding of the denoised codes (the samples whose float code
