@@ -2,7 +2,8 @@
  * The plain FP32 pipeline: the same algorithm as the fused kernels, as one
  * straightforward kernel per stage, one thread per output value, every
  * intermediate a full-resolution FP32 image in device memory and every
- * stencil read through the cache with the mirror computed per tap. It is
+ * stencil read through the cache (mirrored per tap, except that the NLM
+ * reads directly where its whole window lies inside the plane). It is
  * the baseline the fused pipeline is measured against, and a second,
  * independent GPU formulation of the reference's sweeps
  * (lib/ref/ref_denoise.c:168-336, lib/ref/ref_debayer.c:42-395,
@@ -107,24 +108,36 @@ __global__ void p_dn_nlm(const CRAWKDenoise k, const CRAWKDenoiseIO io, const fl
     if (k.mode & CRAW_K_DN_SPATIAL) {
         float acc = 0.0f, wsum = 0.0f;
         const float vc = hist ? vp[(size_t)y * k.pw + x] : 1.0f;
+        /* The plane value at (x + a, y + b): read directly where the whole
+         * 9x9 window lies inside the plane (nearly every sample), mirrored
+         * at the edges. The centre's own patch is read once. */
+        const bool inner = x >= S + P && y >= S + P && x + S + P < k.pw && y + S + P < k.ph;
+        auto val = [&](const float *pp, int a, int b) {
+            return inner ? __ldg(pp + (size_t)(y + b) * k.pw + x + a) : at(pp, k.pw, k.ph, x + a, y + b);
+        };
+        float c[2 * P + 1][2 * P + 1];
+        for (int ky = -P; ky <= P; ky++)
+            for (int kx = -P; kx <= P; kx++)
+                c[ky + P][kx + P] = val(tp, kx, ky);
         for (int dy = -S; dy <= S; dy++) {
             for (int dx = -S; dx <= S; dx++) {
                 float d2 = 0.0f;
+#pragma unroll
                 for (int ky = -P; ky <= P; ky++)
+#pragma unroll
                     for (int kx = -P; kx <= P; kx++) {
-                        float e = at(tp, k.pw, k.ph, x + kx, y + ky) -
-                                  at(tp, k.pw, k.ph, x + dx + kx, y + dy + ky);
+                        float e = c[ky + P][kx + P] - val(tp, dx + kx, dy + ky);
                         d2 += e * e;
                     }
                 float w;
                 if (hist) {
-                    float v2 = vc + at(vp, k.pw, k.ph, x + dx, y + dy);
+                    float v2 = vc + val(vp, dx, dy);
                     w = expf(-fmaxf(d2 * (1.0f / 9.0f) * k.inv_h2 - v2, 0.0f) / vc);
                 } else {
                     w = expf(-fmaxf(d2 * (1.0f / 9.0f) * k.inv_h2 - 2.0f, 0.0f));
                 }
                 wsum += w;
-                acc += w * at(tp, k.pw, k.ph, x + dx, y + dy);
+                acc += w * val(tp, dx, dy);
             }
         }
         u = gat_inv(k, acc / wsum);
