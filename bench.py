@@ -1,7 +1,10 @@
 """Benchmark of the headline workload: full development of 5760x3240 RGGB
 12-bit frames -- VST + NLM 1.0 (7x7 search, 3x3 patch) + RCD + matrix to
-ACES AP1 float32 RGBA (with the ACES 1.3 gamut compression) + the AWB
-histogram -- on one GB300 per process.
+ACES AP1 float32 RGB (with the ACES 1.3 gamut compression) + the AWB
+histogram -- on one GB300 per process. The frame is written as RGB32F
+(three floats a pixel, the config's "float32 RGB"; an extension format of
+this library) by default; ``--out-format rgba32f`` writes the reference's
+RGBA32F (alpha 1), which the side runs also measure.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl fused|plain|reference]
                     [--storage fp32|fp16]
@@ -11,7 +14,7 @@ craw_pipeline_record() (libcraw.so). ``value`` is frames/s with the mosaic
 resident in device memory, from CUDA events around every step on the
 recording stream, L2 flushed (a 256 MB write) between steps; ``e2e`` is
 the same metric through the same call with the mosaic copied in from and
-the RGBA32F frame copied out to pinned host memory inside the timed
+the developed frame copied out to pinned host memory inside the timed
 region. ``roofline`` is the dominant kernel's (the denoise) HBM view and
 ``roofline_fp32`` its FP32-pipe view; ``cpu_baseline`` is the CPU oracle
 (a port of the reference's lib/ref) on the host cores.
@@ -70,15 +73,19 @@ def parse():
                          "(CRAW_PIPELINE_FLAG_EXACT_ROUNDING), which the metric's 1e-3 bound needs; "
                          "float: the reference's float rounding")
     ap.add_argument("--no-extras", action="store_true", help="skip the plain/fp16/cpu side runs")
-    ap.add_argument("--extras", default="plain,fp16,batch,temporal,serve,target,config1,highlights,noise,cpu",
-                    help="comma list of side runs: plain, fp16, batch, temporal, serve, highlights, "
-                         "noise, cpu")
+    ap.add_argument("--extras", default="plain,fp16,rgba32f,batch,temporal,serve,target,config1,highlights,"
+                                        "noise,cpu",
+                    help="comma list of side runs: plain, fp16, rgba32f, batch, temporal, serve, "
+                         "highlights, noise, cpu")
     ap.add_argument("--force-shape", type=int, default=-1,
                     help="denoise tile shape index instead of the autotuner's (profiling)")
     ap.add_argument("--e2e-lanes", type=int, default=0,
                     help="pipelines the end-to-end leg rotates over (0: the default)")
     ap.add_argument("--width", type=int, default=None, help="frame width (default: the workload's)")
     ap.add_argument("--height", type=int, default=None, help="frame height (default: the workload's)")
+    ap.add_argument("--out-format", default="rgb32f", choices=["rgb32f", "rgba32f"],
+                    help="the developed frame's layout: three floats a pixel (the config's float32 "
+                         "RGB) or the reference's four (alpha 1)")
     ap.add_argument("--workload", default="nlm_rcd_ap1",
                     choices=["nlm_rcd_ap1", "batch_rcd_bt2020", "bilinear_bt709_1080p"],
                     help="the timed single-frame workload: the headline (5760x3240 VST + NLM + RCD + "
@@ -271,6 +278,18 @@ def cpu_model() -> str:
     return platform.machine()
 
 
+def out_image(L, w, h, fmt):
+    """A device image for the developed frame: (tensor, craw image). RGB32F
+    rows are w * 12 bytes rounded up to 16 (the tensor a view of them)."""
+    import torch
+    if fmt == L.FORMAT_RGB32F:
+        pitch = (w * 12 + 15) // 16 * 16
+        buf = torch.empty((h, pitch // 4), dtype=torch.float32, device="cuda")
+        return buf[:, : 3 * w].view(h, w, 3), L.Image(buf.data_ptr(), pitch, fmt, w, h)
+    t = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
+    return t, L.Image(t.data_ptr(), w * 16, fmt, w, h)
+
+
 def run_reference(args):
     # Rank 0 alone runs the CPU baseline; the other ranks have no work.
     if int(os.environ.get("RANK", "0")) != 0:
@@ -344,8 +363,8 @@ def run_gpu(args):
                                  noise_a_dn=c.noise_a_dn, noise_b_dn=c.noise_b_dn) for i in range(nfr)]
     dev_frames = [torch.from_numpy(f.view(np.int16)).cuda() for f in host_frames]
     srcs = [L.Image(t.data_ptr(), w * 2, L.FORMAT_R16_UNORM, w, h) for t in dev_frames]
-    out = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
-    dst = L.Image(out.data_ptr(), w * 16, L.FORMAT_RGBA32F, w, h)
+    out_fmt = L.FORMAT_RGB32F if args.out_format == "rgb32f" else L.FORMAT_RGBA32F
+    out, dst = out_image(L, w, h, out_fmt)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
     ctx = L.Context(dev)
@@ -357,14 +376,14 @@ def run_gpu(args):
 
     exact = args.rounding == "exact" and impl == L.IMPL_FUSED
 
-    def make_pipe(impl_, storage_, profile=True, exact_=None):
+    def make_pipe(impl_, storage_, profile=True, exact_=None, fmt=None):
         exact_ = exact if exact_ is None else exact_
         flags = c.flags | (L.FLAG_PROFILE if profile else 0) | (L.FLAG_EXACT_ROUNDING if exact_ else 0)
         return L.Pipeline(ctx, L.pipeline_params(w, h, debayer=c.debayer, out_space=c.out_space,
-                                                 flags=flags, out_format=L.FORMAT_RGBA32F,
+                                                 flags=flags, out_format=fmt or out_fmt,
                                                  storage=storage_, impl=impl_, nb_awb_slots=2))
 
-    def timed(pipe, steps, warmup, collect=True):
+    def timed(pipe, steps, warmup, collect=True, dst=dst):
         with torch.cuda.stream(stream):
             for i in range(warmup):
                 pipe.record(sptr, srcs[i % nfr], dst, fp)
@@ -436,51 +455,57 @@ def run_gpu(args):
                             f"{roof32['frac']:.2f} of the FP32 lane rate (roofline_fp32), "
                             f"{roof['frac']:.3f} of HBM")
 
-    # End to end through the same call: pinned host mosaic in, RGBA32F out.
-    # E2E_LANES lanes (pipeline + CUDA stream + device buffers each) take
-    # the steps in turn, so one frame's copy in, another's kernels and
+    # End to end through the same call: pinned host mosaic in, the frame
+    # out. E2E_LANES lanes (pipeline + CUDA stream + device buffers each)
+    # take the steps in turn, so one frame's copy in, another's kernels and
     # others' copies out overlap, as a caller streaming frames would.
     pinned_in = [torch.from_numpy(f.view(np.int16)).pin_memory() for f in host_frames]
-    lanes = []
-    for _ in range(E2E_LANES):
-        ls = torch.cuda.Stream()
-        d_in = torch.empty((h, w), dtype=torch.int16, device="cuda")
-        d_out = torch.empty((h, w, 4), dtype=torch.float32, device="cuda")
-        lanes.append(dict(stream=ls, d_in=d_in, d_out=d_out,
-                          h_out=torch.empty((h, w, 4), dtype=torch.float32).pin_memory(),
-                          src=L.Image(d_in.data_ptr(), w * 2, L.FORMAT_R16_UNORM, w, h),
-                          dst=L.Image(d_out.data_ptr(), w * 16, L.FORMAT_RGBA32F, w, h),
-                          pipe=make_pipe(impl, storage, profile=False)))
 
-    def e2e_step(i, nl):
-        ln = lanes[i % nl]
-        with torch.cuda.stream(ln["stream"]):
-            ln["d_in"].copy_(pinned_in[i % nfr], non_blocking=True)
-            ln["pipe"].record(ln["stream"].cuda_stream, ln["src"], ln["dst"], fp)
-            ln["h_out"].copy_(ln["d_out"], non_blocking=True)
+    def run_e2e(fmt):
+        lanes = []
+        for _ in range(E2E_LANES):
+            ls = torch.cuda.Stream()
+            d_in = torch.empty((h, w), dtype=torch.int16, device="cuda")
+            d_out, d_img = out_image(L, w, h, fmt)
+            lanes.append(dict(stream=ls, d_in=d_in, d_buf=d_out._base if d_out._base is not None else d_out,
+                              src=L.Image(d_in.data_ptr(), w * 2, L.FORMAT_R16_UNORM, w, h), dst=d_img,
+                              pipe=make_pipe(impl, storage, profile=False, fmt=fmt)))
+            ln = lanes[-1]
+            ln["h_buf"] = torch.empty(ln["d_buf"].shape, dtype=ln["d_buf"].dtype).pin_memory()
 
-    def e2e_run(nl):
-        for i in range(3 * nl):
-            e2e_step(i, nl)
-        torch.cuda.synchronize()
-        barrier(ws)
-        t0 = time.perf_counter()
-        for i in range(args.steps):
-            e2e_step(i, nl)
-        torch.cuda.synchronize()
-        return max_over_ranks(time.perf_counter() - t0, ws)
+        def e2e_step(i, nl):
+            ln = lanes[i % nl]
+            with torch.cuda.stream(ln["stream"]):
+                ln["d_in"].copy_(pinned_in[i % nfr], non_blocking=True)
+                ln["pipe"].record(ln["stream"].cuda_stream, ln["src"], ln["dst"], fp)
+                ln["h_buf"].copy_(ln["d_buf"], non_blocking=True)
 
-    e2e_s1 = e2e_run(1)
-    e2e_s = e2e_run(len(lanes))
-    e2e = {"value": ws * args.steps / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": w * h * 2,
-           "d2h_bytes_per_step": w * h * 16,
-           "one_stream_value": ws * args.steps / e2e_s1,
-           "how": "per step: H2D of the mosaic from pinned memory, craw_pipeline_record, D2H of "
-                  f"the RGBA32F frame to pinned memory, on one of {E2E_LANES} streams in turn (each with its "
-                  "own pipeline and buffers); wall clock over all steps; one_stream_value: all "
-                  "steps on one stream"}
-    for ln in lanes:
-        ln["pipe"].close()
+        def e2e_run(nl):
+            for i in range(3 * nl):
+                e2e_step(i, nl)
+            torch.cuda.synchronize()
+            barrier(ws)
+            t0 = time.perf_counter()
+            for i in range(args.steps):
+                e2e_step(i, nl)
+            torch.cuda.synchronize()
+            return max_over_ranks(time.perf_counter() - t0, ws)
+
+        e2e_s1 = e2e_run(1)
+        e2e_s = e2e_run(len(lanes))
+        name = "RGB32F" if fmt == L.FORMAT_RGB32F else "RGBA32F"
+        res = {"value": ws * args.steps / e2e_s, "unit": "frames/s", "h2d_bytes_per_step": w * h * 2,
+               "d2h_bytes_per_step": lanes[0]["h_buf"].numel() * 4,
+               "one_stream_value": ws * args.steps / e2e_s1,
+               "how": "per step: H2D of the mosaic from pinned memory, craw_pipeline_record, D2H of "
+                      f"the {name} frame to pinned memory, on one of {E2E_LANES} streams in turn (each with "
+                      "its own pipeline and buffers); wall clock over all steps; one_stream_value: all "
+                      "steps on one stream"}
+        for ln in lanes:
+            ln["pipe"].close()
+        return res
+
+    e2e = run_e2e(out_fmt)
 
     extras = {}
     want = set() if args.no_extras else set(args.extras.split(","))
@@ -495,6 +520,15 @@ def run_gpu(args):
             with make_pipe(im, st, profile=False) as p2:
                 m2, _, _ = timed(p2, max(5, args.steps // 3), 3, collect=False)
             extras[name] = {"fps": 1000.0 / statistics.mean(m2), "ms_per_frame": statistics.mean(m2)}
+        if "rgba32f" in want and out_fmt != L.FORMAT_RGBA32F:
+            # The reference's output layout, four floats a pixel (alpha 1):
+            # a quarter more bytes written, and copied to the host.
+            o4, d4 = out_image(L, w, h, L.FORMAT_RGBA32F)
+            with make_pipe(impl, storage, profile=False, fmt=L.FORMAT_RGBA32F) as p2:
+                m2, _, _ = timed(p2, max(5, args.steps // 3), 3, collect=False, dst=d4)
+            del o4
+            extras["rgba32f_output"] = {"fps": 1000.0 / statistics.mean(m2), "ms_per_frame": statistics.mean(m2),
+                                        "e2e": run_e2e(L.FORMAT_RGBA32F)}
         if exact:
             # The same pipeline with the reference's float rounding of the
             # denoised codes (about 0.03 % of them one code from an FP64
@@ -546,6 +580,8 @@ def run_gpu(args):
             "data": "synthetic: seeded generator (gradient + 256 rectangles + 4 zone plates, "
                     "Poisson-Gaussian noise a=4 DN, b=40 DN^2), 4 frames in rotation",
             "config": {"workload": label, "width": w, "height": h, "impl": args.impl,
+                       "output": "RGB32F (three floats a pixel)" if out_fmt == L.FORMAT_RGB32F
+                                 else "RGBA32F (four floats a pixel, alpha 1)",
                        "storage": args.storage, "l2": "flushed between steps (256 MB write)",
                        "rounding": ("exact: denoised codes as an FP64 evaluation rounds them"
                                     if exact else "float (the reference's)"),
@@ -556,10 +592,11 @@ def run_gpu(args):
             "stage_ms": {k: statistics.mean(v) for k, v in stage.items()},
             "roofline": roof, "roofline_fp32": roof32,
             "e2e": e2e,
-            # Our kernels per step: fused = denoise, [the rounding's decision and
-            # double-float kernels,] RCD quad tiles, RCD border tiles, awb_reduce;
-            # plain = vst + nlm, prep + 8 RCD sweeps + awb + colour.
-            "gpu_launches": args.steps * ((6 if exact else 4) if impl == L.IMPL_FUSED else 13),
+            # Our kernels per step: fused = denoise, [the rounding's compaction,
+            # decision and double-float kernels,] RCD interior (tiles or strips),
+            # RCD border tiles, awb_reduce; plain = vst + nlm, prep + 8 RCD
+            # sweeps + awb + colour.
+            "gpu_launches": args.steps * ((7 if exact else 4) if impl == L.IMPL_FUSED else 13),
             "clocks": {k: clk_s[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
             "awb_samples": int(hist.count.sum()),
             "wall_s_timed": wall,

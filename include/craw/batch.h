@@ -34,7 +34,7 @@ typedef struct CRAWBatchParams {
     uint32_t max_width, max_height;  /* the largest frame (even) */
     enum CRAWDebayer debayer;        /* all frames of a batch */
     enum CRAWColorSpace out_space;   /* default; a frame may override it */
-    CRAWFormat out_format;           /* CRAW_FORMAT_RGBA16F or CRAW_FORMAT_RGBA32F */
+    CRAWFormat out_format;           /* CRAW_FORMAT_RGBA16F, CRAW_FORMAT_RGBA32F or RGB32F */
     uint32_t flags;                  /* CRAW_PIPELINE_FLAG_DENOISE, CRAW_BATCH_FLAG_* */
     /* Frames of at least this many pixels are developed by the single-frame
      * kernels, launched one frame after another on the recording's stream

@@ -23,6 +23,10 @@ typedef enum CRAWFormat {
     CRAW_FORMAT_R16F      = 76,   /* one half float per sample (VK_FORMAT_R16_SFLOAT): the
                                    * rebuilt highlight mosaic, read back for tests only */
     CRAW_FORMAT_RGBA16F   = 97,   /* four IEEE half floats per pixel */
+    CRAW_FORMAT_RGB32F    = 106,  /* three IEEE floats per pixel, no alpha
+                                   * (VK_FORMAT_R32G32B32_SFLOAT); an extension for
+                                   * outputs that leave the device: a quarter fewer bytes
+                                   * than RGBA32F, rows 16-byte aligned as every image's */
     CRAW_FORMAT_RGBA32F   = 109,  /* four IEEE floats per pixel */
 } CRAWFormat;
 

@@ -123,7 +123,8 @@ typedef struct CRAWPipelineParams {
     enum CRAWCfa cfa;           /* CRAW_CFA_RGGB */
     enum CRAWDebayer debayer;
     enum CRAWColorSpace out_space;   /* default; a frame may override it */
-    CRAWFormat out_format;      /* CRAW_FORMAT_RGBA16F or CRAW_FORMAT_RGBA32F */
+    CRAWFormat out_format;      /* CRAW_FORMAT_RGBA16F, CRAW_FORMAT_RGBA32F or (an extension)
+                                 * CRAW_FORMAT_RGB32F */
     uint32_t flags;             /* CRAW_PIPELINE_FLAG_* */
     uint32_t nb_awb_slots;      /* host-visible histogram copies, 1..4 (0 = 1) */
 

@@ -40,6 +40,8 @@ DEBAYER_BILINEAR, DEBAYER_MHC, DEBAYER_RCD = 0, 1, 2
  CS_ACES_AP1) = range(7)
 FORMAT_R16_UNORM, FORMAT_RGBA16F, FORMAT_RGBA32F = 70, 97, 109
 FORMAT_R16F = 76
+#: Three floats a pixel, no alpha (an extension of this library).
+FORMAT_RGB32F = 106
 WB_AS_SHOT, WB_REBALANCE = 0, 1
 STORAGE_FP32, STORAGE_FP16 = 0, 1
 IMPL_FUSED, IMPL_PLAIN = 0, 1

@@ -220,7 +220,7 @@ CRAW_API int craw_batch_create(CRAWContext *ctx, const CRAWBatchParams *params, 
         params->max_width < 12 || params->max_height < 12 || params->max_width > 32768 ||
         params->max_height > 32768 || (unsigned)params->debayer >= CRAW_DEBAYER_NB ||
         (unsigned)params->out_space >= CRAW_CS_NB ||
-        (params->out_format != CRAW_FORMAT_RGBA16F && params->out_format != CRAW_FORMAT_RGBA32F))
+        !craw_is_out_format(params->out_format))
         return CRAW_ERROR(EINVAL);
     if ((params->flags & ~(uint32_t)(CRAW_PIPELINE_FLAG_DENOISE | CRAW_BATCH_FLAG_UNFUSED |
                                       CRAW_BATCH_FLAG_FUSED | CRAW_BATCH_FLAG_NO_GRAPH)) ||
@@ -379,7 +379,7 @@ CRAW_API int craw_batch_record(CRAWBatch *b, cudaStream_t s, uint32_t nb, const 
         F[i].vio.src_pitch = dn[i] ? b->clean_pitch : src[i].pitch;
         F[i].vio.dst = dst[i].data;
         F[i].vio.dst_pitch = dst[i].pitch;
-        F[i].vio.dst_half = dst[i].format == CRAW_FORMAT_RGBA16F;
+        F[i].vio.dst_fmt = craw_out_layout(dst[i].format);
     }
 
     /* Large frames go to the single-frame kernels; the others, in order,

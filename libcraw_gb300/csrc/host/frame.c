@@ -15,10 +15,32 @@
 #define DN_GUARD_LO 0.90f
 #define DN_GUARD_HI 1.00f
 
+size_t craw_format_bpp(CRAWFormat fmt)
+{
+    switch (fmt) {
+    case CRAW_FORMAT_R16_UNORM:
+    case CRAW_FORMAT_R16F:    return 2;
+    case CRAW_FORMAT_RGBA16F: return 8;
+    case CRAW_FORMAT_RGB32F:  return 12;
+    default:                  return 16;
+    }
+}
+
+bool craw_is_out_format(CRAWFormat fmt)
+{
+    return fmt == CRAW_FORMAT_RGBA16F || fmt == CRAW_FORMAT_RGBA32F || fmt == CRAW_FORMAT_RGB32F;
+}
+
+int craw_out_layout(CRAWFormat fmt)
+{
+    return fmt == CRAW_FORMAT_RGBA16F ? CRAW_K_OUT_RGBA16F
+         : fmt == CRAW_FORMAT_RGB32F  ? CRAW_K_OUT_RGB32F : CRAW_K_OUT_RGBA32F;
+}
+
 int craw_image_check(CRAWContext *ctx, const CRAWImage *img, CRAWFormat fmt, uint32_t w, uint32_t h,
                      const char *what)
 {
-    size_t bpp = fmt == CRAW_FORMAT_R16_UNORM ? 2 : (fmt == CRAW_FORMAT_RGBA16F ? 8 : 16);
+    size_t bpp = craw_format_bpp(fmt);
     if (img->format != fmt) {
         craw_log(ctx, CRAW_LOG_ERROR, "%s format %d, expected %d\n", what, (int)img->format, (int)fmt);
         return CRAW_ERROR(EINVAL);

@@ -41,6 +41,12 @@ int craw_dev_sync(CRAWContext *ctx);
 extern int craw_forced_denoise_shape;
 
 /* Per-frame constants (frame.c). */
+/* Bytes a pixel of an image format takes; whether a format can be an
+ * output of the colour stage (RGBA16F, RGBA32F, RGB32F); and the kernels'
+ * CRAW_K_OUT_* layout of such a format. */
+size_t craw_format_bpp(CRAWFormat fmt);
+bool craw_is_out_format(CRAWFormat fmt);
+int craw_out_layout(CRAWFormat fmt);
 int craw_image_check(CRAWContext *ctx, const CRAWImage *img, CRAWFormat fmt, uint32_t w, uint32_t h,
                      const char *what);
 bool craw_images_overlap(const CRAWImage *a, const CRAWImage *b);

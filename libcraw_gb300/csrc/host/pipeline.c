@@ -447,8 +447,8 @@ CRAW_API int craw_pipeline_create(CRAWContext *ctx, const CRAWPipelineParams *pa
         craw_log(ctx, CRAW_LOG_ERROR, "Frame size %ux%u is larger than 32768 on a side\n", w, h);
         return CRAW_ERROR(EINVAL);
     }
-    if (params->out_format != CRAW_FORMAT_RGBA16F && params->out_format != CRAW_FORMAT_RGBA32F) {
-        craw_log(ctx, CRAW_LOG_ERROR, "Output format must be RGBA16F or RGBA32F\n");
+    if (!craw_is_out_format(params->out_format)) {
+        craw_log(ctx, CRAW_LOG_ERROR, "Output format must be RGBA16F, RGBA32F or RGB32F\n");
         return CRAW_ERROR(EINVAL);
     }
     if ((unsigned)params->debayer >= CRAW_DEBAYER_NB || (unsigned)params->out_space >= CRAW_CS_NB ||
@@ -831,7 +831,7 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
     if (p->plain) {
         dio.dst = dst->data;
         dio.dst_pitch = dst->pitch;
-        dio.dst_half = dst->format == CRAW_FORMAT_RGBA16F;
+        dio.dst_fmt = craw_out_layout(dst->format);
         prof_begin(&pc, ST_DEVELOP);
         ret = craw_k_plain_develop(&dk, &dio, chroma ? &ck : NULL, p->p_v, p->inter, p->inter_pitch,
                                    p->p_scratch, p->q, p->qf, p->awb ? (uint32_t *)awb_hist : NULL, s);
@@ -841,7 +841,7 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
     } else if (!chroma) {
         dio.dst = dst->data;
         dio.dst_pitch = dst->pitch;
-        dio.dst_half = dst->format == CRAW_FORMAT_RGBA16F;
+        dio.dst_fmt = craw_out_layout(dst->format);
         if (p->keep) {
             dio.inter = p->inter;
             dio.inter_pitch = p->inter_pitch;
@@ -870,7 +870,7 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
             goto launch_fail;
         prof_begin(&pc, ST_UP);
         ret = craw_k_chroma_up_color(&dk, &ck, p->inter, p->inter_pitch, p->q, p->qf, p->q_pitch,
-                                     dst->data, dst->pitch, dst->format == CRAW_FORMAT_RGBA16F,
+                                     dst->data, dst->pitch, craw_out_layout(dst->format),
                                      p->keep ? p->inter : NULL, &awb, s);
         prof_end(&pc);
         if (ret < 0)

@@ -531,7 +531,7 @@ CRAW_API int craw_server_stream_open(CRAWServer *s, const CRAWServerStreamParams
     if (!s || !params || !stream_id)
         return CRAW_ERROR(EINVAL);
     pp = &params->pipeline;
-    if (pp->out_format != CRAW_FORMAT_RGBA16F && pp->out_format != CRAW_FORMAT_RGBA32F)
+    if (!craw_is_out_format(pp->out_format))
         return CRAW_ERROR(EINVAL);
     if ((params->flags & ~(CRAW_SERVER_STREAM_AUTO_WB | CRAW_SERVER_STREAM_ESTIMATE_NOISE)) ||
         ((params->flags & CRAW_SERVER_STREAM_AUTO_WB) && !(pp->flags & CRAW_PIPELINE_FLAG_AWB_HISTOGRAM))) {
@@ -546,7 +546,7 @@ CRAW_API int craw_server_stream_open(CRAWServer *s, const CRAWServerStreamParams
     if (!(st = calloc(1, sizeof(*st))))
         return CRAW_ERROR(ENOMEM);
     st->params = *params;
-    st->bpp = pp->out_format == CRAW_FORMAT_RGBA16F ? 8 : 16;
+    st->bpp = (uint32_t)craw_format_bpp(pp->out_format);
     st->nb_slots = s->params.slots_per_stream;
 
     pthread_mutex_lock(&s->open_lock);

@@ -190,11 +190,18 @@ typedef struct CRAWKAwbOut {
     uint32_t *nb_deferred;         /* counter, zeroed before the frame */
 } CRAWKAwbOut;
 
+/* Layouts of an RGB image a kernel stores: four floats (alpha 1), four
+ * half floats (alpha 1), three floats. */
+#define CRAW_K_OUT_RGBA32F 0
+#define CRAW_K_OUT_RGBA16F 1
+#define CRAW_K_OUT_RGB32F 2
+
 typedef struct CRAWKDevelopIO {
     const uint16_t *src; size_t src_pitch;
     int32_t src_f16;                                    /* src holds fp16 values already
                                                          * prepped (the rebuilt highlights) */
-    void *dst; size_t dst_pitch; int32_t dst_half;      /* NULL: no colour stage */
+    void *dst; size_t dst_pitch; int32_t dst_fmt;       /* NULL: no colour stage; dst_fmt a
+                                                         * CRAW_K_OUT_* layout */
     void *inter; size_t inter_pitch;                    /* NULL: not kept */
     void *quarter; size_t quarter_pitch;                /* chroma: block means out */
     CRAWKAwbOut awb;
@@ -245,7 +252,7 @@ int craw_k_chroma_blur(const CRAWKChroma *c, const void *q, size_t q_pitch,
 int craw_k_chroma_up_color(const CRAWKDevelop *k, const CRAWKChroma *c,
                            const void *inter, size_t inter_pitch,
                            const void *q, const void *qf, size_t q_pitch,
-                           void *dst, size_t dst_pitch, int dst_half,
+                           void *dst, size_t dst_pitch, int dst_fmt,
                            void *inter_out, const CRAWKAwbOut *awb, cudaStream_t s);
 
 /* ---------------------------------------------------------------- awb */

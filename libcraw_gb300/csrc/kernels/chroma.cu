@@ -72,7 +72,7 @@ constexpr int TW = 64, TH = 32, NT = 256;
 __global__ void __launch_bounds__(NT)
 k_chroma_up_color(const CRAWKDevelop k, const CRAWKChroma c, const void *inter, size_t inter_pitch,
                   const void *q, const void *qf, size_t q_pitch, void *dst, size_t dst_pitch,
-                  int dst_half, void *inter_out, const CRAWKAwbOut awb)
+                  int dst_fmt, void *inter_out, const CRAWKAwbOut awb)
 {
     __shared__ __align__(16) float rgb_s[3 * TW * TH];
     static_assert(TW % 8 == 0, "block rows are whole float4s");
@@ -117,7 +117,7 @@ k_chroma_up_color(const CRAWKDevelop k, const CRAWKChroma c, const void *inter, 
             craw_store_rgba(inter_out, inter_pitch, x, y, c.fp16, o[0], o[1], o[2]);
         float co[3];
         craw_color(k.color, o, co);
-        craw_store_rgba(dst, dst_pitch, x, y, dst_half, co[0], co[1], co[2]);
+        craw_store_rgba(dst, dst_pitch, x, y, dst_fmt, co[0], co[1], co[2]);
     }
     if (!awb.rec)
         return;
@@ -180,13 +180,13 @@ extern "C" int craw_k_chroma_blur(const CRAWKChroma *c, const void *q, size_t q_
 extern "C" int craw_k_chroma_up_color(const CRAWKDevelop *k, const CRAWKChroma *c,
                                       const void *inter, size_t inter_pitch,
                                       const void *q, const void *qf, size_t q_pitch,
-                                      void *dst, size_t dst_pitch, int dst_half,
+                                      void *dst, size_t dst_pitch, int dst_fmt,
                                       void *inter_out, const CRAWKAwbOut *awb, cudaStream_t s)
 {
     if (craw_launch_ready() < 0)
         return -5;
     dim3 grid((c->width + TW - 1) / TW, (c->height + TH - 1) / TH);
     k_chroma_up_color<<<grid, NT, 0, s>>>(*k, *c, inter, inter_pitch, q, qf, q_pitch, dst,
-                                          dst_pitch, dst_half, inter_out, *awb);
+                                          dst_pitch, dst_fmt, inter_out, *awb);
     return cudaGetLastError() == cudaSuccess ? 0 : -5;
 }

@@ -205,11 +205,18 @@ CRAW_DEV void craw_color(const CRAWKColor &c, const float in[3], float o[3])
     }
 }
 
-CRAW_DEV void craw_store_rgba(void *base, size_t pitch, int x, int y, int half_fmt,
+/* Pixel (x, y) of an RGB image of layout `fmt` (CRAW_K_OUT_*: 0 four
+ * floats, 1 four half floats, 2 three floats). */
+CRAW_DEV void craw_store_rgba(void *base, size_t pitch, int x, int y, int fmt,
                               float r, float g, float b)
 {
     char *row = (char *)base + (size_t)y * pitch;
-    if (half_fmt) {
+    if (fmt == CRAW_K_OUT_RGB32F) {
+        float *p = reinterpret_cast<float *>(row) + 3 * (size_t)x;
+        p[0] = r;
+        p[1] = g;
+        p[2] = b;
+    } else if (fmt == CRAW_K_OUT_RGBA16F) {
         __half2 lo = __floats2half2_rn(r, g), hi = __floats2half2_rn(b, 1.0f);
         uint2 v;
         v.x = *reinterpret_cast<uint32_t *>(&lo);

@@ -202,7 +202,7 @@ CRAW_DEV void rcd_strip(const CRAWKDevelop &k, const CRAWKDevelopIO &io, const S
             if (io.dst) {
                 float q[3];
                 craw_color(k.color, v, q);
-                craw_store_rgba(io.dst, io.dst_pitch, px, py, io.dst_half, q[0], q[1], q[2]);
+                craw_store_rgba(io.dst, io.dst_pitch, px, py, io.dst_fmt, q[0], q[1], q[2]);
             }
         }
     };

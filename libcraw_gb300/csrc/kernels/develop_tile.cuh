@@ -676,7 +676,7 @@ CRAW_DEV void epilogue(const CRAWKDevelop &k, const CRAWKDevelopIO &io, int x0, 
         if (!chroma && io.dst) {
             float o[3];
             craw_color(k.color, v, o);
-            craw_store_rgba(io.dst, io.dst_pitch, x, y, io.dst_half, o[0], o[1], o[2]);
+            craw_store_rgba(io.dst, io.dst_pitch, x, y, io.dst_fmt, o[0], o[1], o[2]);
         }
     }
     if ((!chroma && !io.awb.rec) || awb_apart)

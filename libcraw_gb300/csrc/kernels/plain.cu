@@ -505,6 +505,6 @@ extern "C" int craw_k_plain_develop(const CRAWKDevelop *k, const CRAWKDevelopIO 
     if (hist)
         p_awb<<<GRID2((w + 7) / 8, (h + 7) / 8), 0, s>>>(*k, inter, ip, hist, io->awb);
     if (io->dst)
-        p_color<<<GRID2(w, h), 0, s>>>(*k, inter, ip, io->dst, io->dst_pitch, io->dst_half);
+        p_color<<<GRID2(w, h), 0, s>>>(*k, inter, ip, io->dst, io->dst_pitch, io->dst_fmt);
     return LAUNCH_OK;
 }

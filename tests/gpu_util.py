@@ -21,6 +21,14 @@ def upload_mosaic(m: np.ndarray) -> tuple[torch.Tensor, L.Image]:
 
 
 def alloc_rgba(w: int, h: int, fmt: int = L.FORMAT_RGBA32F) -> tuple[torch.Tensor, L.Image]:
+    """A device image of an output format: (h, w, 4) for RGBA32F / RGBA16F,
+    (h, w, 3) for RGB32F (rows padded to 16 bytes, the tensor a view of
+    them)."""
+    if fmt == L.FORMAT_RGB32F:
+        pitch = (w * 12 + 15) // 16 * 16
+        buf = torch.full((h, pitch // 4), float("nan"), dtype=torch.float32, device="cuda")
+        t = buf[:, : 3 * w].view(h, w, 3)
+        return t, L.Image(buf.data_ptr(), pitch, fmt, w, h)
     dt = torch.float32 if fmt == L.FORMAT_RGBA32F else torch.float16
     t = torch.full((h, w, 4), float("nan"), dtype=dt, device="cuda")
     return t, L.Image(t.data_ptr(), t.stride(0) * t.element_size(), fmt, w, h)
