@@ -794,7 +794,7 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
         CRAWKHighlightIO hio = {
             .src = mosaic, .src_pitch = mosaic_pitch,
             .dst = p->hl_mosaic, .dst_pitch = p->hl_pitch,
-            .levels = p->hl_levels,
+            .levels = p->hl_levels, .err = p->kerr,
         };
         hk.width = (int32_t)w;
         hk.height = (int32_t)h;
@@ -827,6 +827,7 @@ CRAW_API int craw_pipeline_record(CRAWPipeline *p, cudaStream_t s, const CRAWIma
     ck.qh = p->qh;
     ck.strength = fp->denoise_chroma_strength;
     ck.fp16 = p->fp16;
+    ck.err = p->kerr;
 
     if (p->plain) {
         dio.dst = dst->data;

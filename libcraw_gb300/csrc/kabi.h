@@ -241,6 +241,7 @@ typedef struct CRAWKChroma {
     int32_t width, height, qw, qh;
     float strength;
     int32_t fp16;
+    uint32_t *err;                  /* device word for CRAW_K_ERR_* bits; NULL: none */
 } CRAWKChroma;
 
 /* 9x9 joint bilateral on the quarter grid: q -> qf. */
@@ -282,6 +283,7 @@ typedef struct CRAWKHighlightIO {
     const uint16_t *src; size_t src_pitch;
     uint16_t *dst; size_t dst_pitch;  /* fp16 bits, balanced mosaic */
     void *levels;                   /* float4 texels (c0, c1, weight, 0) */
+    uint32_t *err;                  /* device word for CRAW_K_ERR_* bits; NULL: none */
 } CRAWKHighlightIO;
 
 /* Level sizes and offsets of a width x height frame into `k`; returns the

@@ -27,14 +27,15 @@ k_chroma_blur(const CRAWKChroma c, const void *q, size_t q_pitch, void *qf, size
     const int x0 = blockIdx.x * BX, y0 = blockIdx.y * BY;
     for (int i = threadIdx.x; i < (BY + 2 * kR) * SX; i += BX * BY) {
         int x = craw_mirror(x0 - kR + i % SX, c.qw), y = craw_mirror(y0 - kR + i / SX, c.qh);
-        float v[3];
-        craw_load_rgb(q, q_pitch, x, y, c.fp16, v);
+        float v[3] = { 0.0f, 0.0f, 0.0f };
+        if (craw_in_bounds(x >= 0 && x < c.qw && y >= 0 && y < c.qh, c.err))
+            craw_load_rgb(q, q_pitch, x, y, c.fp16, v);
         t[i] = make_float4(v[0], v[1], v[2], 0.0f);
     }
     __syncthreads();
     const int lx = threadIdx.x % BX, ly = threadIdx.x / BX;
     const int x = x0 + lx, y = y0 + ly;
-    if (x >= c.qw || y >= c.qh)
+    if (x >= c.qw || y >= c.qh || !craw_in_bounds(x >= 0 && y >= 0, c.err))
         return;
     const float4 ctr = t[(ly + kR) * SX + lx + kR];
     const float level = fmaxf(ctr.z, 0.0f) + kRangeEps;
@@ -86,6 +87,8 @@ k_chroma_up_color(const CRAWKDevelop k, const CRAWKChroma c, const void *inter, 
         float fx = ((float)x + 0.5f) * 0.25f - 0.5f, flx = floorf(fx), tx = fx - flx;
         int ya = min(max((int)fly, 0), c.qh - 1), yb = min(max((int)fly + 1, 0), c.qh - 1);
         int xa = min(max((int)flx, 0), c.qw - 1), xb = min(max((int)flx + 1, 0), c.qw - 1);
+        if (!craw_in_bounds(x >= 0 && y >= 0 && xa >= 0 && ya >= 0 && xb < c.qw && yb < c.qh, c.err))
+            continue;
         float w00 = (1.0f - tx) * (1.0f - ty), w10 = tx * (1.0f - ty);
         float w01 = (1.0f - tx) * ty, w11 = tx * ty;
         float d00[3], d10[3], d01[3], d11[3], b00[3], b10[3], b01[3], b11[3], px[3];
@@ -159,7 +162,10 @@ k_chroma_up_color(const CRAWKDevelop k, const CRAWKChroma c, const void *inter, 
                 }
         }
         float n = (float)(xe * ye);
-        awb.rec[(size_t)(y0 / 8 + by) * blocks_x + x0 / 8 + bx] =
+        const size_t ri = (size_t)(y0 / 8 + by) * blocks_x + x0 / 8 + bx;
+        if (!craw_in_bounds(ri < craw_awb_blocks(k.width, k.height), c.err))
+            continue;
+        awb.rec[ri] =
             craw_awb_block(__fdiv_rn(s0, n), __fdiv_rn(s1, n), __fdiv_rn(s2, n), k.awb_wb,
                            awb.deferred, awb.nb_deferred, craw_awb_blocks(k.width, k.height));
     }

@@ -50,11 +50,6 @@ CRAW_DEV float site_u(const CRAWKHighlight &k, uint16_t raw, int s)
     return ((float)raw * (1.0f / 65535.0f) - k.black[s]) * k.inv_range[s];
 }
 
-CRAW_DEV uint16_t sample(const CRAWKHighlightIO &io, int x, int y)
-{
-    return __ldg(reinterpret_cast<const uint16_t *>((const char *)io.src + (size_t)y * io.src_pitch) + x);
-}
-
 CRAW_DEV float fmax0(float m, float v) { return m > v ? m : v; }   /* the reference's MAX(m, v) */
 
 CRAW_DEV float clampf(float v, float lo, float hi)
@@ -350,9 +345,12 @@ __global__ void __launch_bounds__(kFillThreads) k_hl_fill(const CRAWKHighlight k
     for (int it = 0; it < kStIt; it++) {
         const int i = tid + it * kFillThreads, r = i / kStPairs, xa = X0 - 2 + 2 * (i - r * kStPairs);
         if (i < kStN) {
+            const int yr = edge(Y0 - 1 + r, k.height);
             const uint16_t *row = reinterpret_cast<const uint16_t *>(
-                (const char *)io.src + (size_t)edge(Y0 - 1 + r, k.height) * io.src_pitch);
-            if (xa >= 0 && xa < k.width)
+                (const char *)io.src + (size_t)yr * io.src_pitch);
+            if (!craw_in_bounds(yr >= 0 && yr < k.height, io.err))
+                raw[it] = 0u;
+            else if (xa >= 0 && xa + 1 < k.width)
                 raw[it] = __ldg(reinterpret_cast<const uint32_t *>(row + xa));
             else
                 raw[it] = (uint32_t)__ldg(row + edge(xa, k.width)) |
@@ -452,7 +450,8 @@ __global__ void __launch_bounds__(kFillThreads) k_hl_fill(const CRAWKHighlight k
 #pragma unroll
     for (int r = 0; r < 2; r++) {
         __half2 hv = __floats2half2_rn(out[r][0], out[r][1]);
-        *reinterpret_cast<__half2 *>((char *)io.dst + (size_t)(y0 + r) * io.dst_pitch + (size_t)x0 * 2) = hv;
+        if (craw_in_bounds(x0 >= 0 && x0 + 1 < k.width && y0 + r >= 0 && y0 + r < k.height, io.err))
+            *reinterpret_cast<__half2 *>((char *)io.dst + (size_t)(y0 + r) * io.dst_pitch + (size_t)x0 * 2) = hv;
     }
 }
 

@@ -1,7 +1,8 @@
 """Frames developed through whichever build of libcraw.so this process
 loaded (CRAW_LIBRARY): the cases the bounds-checked build is run on, from
 the reference's minimum sizes to frames whose tiles, strips and segments
-end short, over every kernel the checks cover. `python bounds_cases.py
+end short, over every kernel the checks cover (develop, denoise, chroma,
+highlight reconstruction). `python bounds_cases.py
 OUT.npz` writes each case's output and the kernel error bits of its
 pipeline."""
 from __future__ import annotations
@@ -29,9 +30,11 @@ CASES = [
      L.FLAG_DENOISE | L.FLAG_AWB_HISTOGRAM | L.FLAG_EXACT_ROUNDING, dict(denoise_strength=1.0), 1),
     ("tiles_ap1", 1286, 718, L.DEBAYER_RCD, L.CS_ACES_AP1, L.FLAG_DENOISE | L.FLAG_AWB_HISTOGRAM,
      dict(denoise_strength=1.0), 1),
-    ("temporal_mhc", 390, 262, L.DEBAYER_MHC, L.CS_P3D65,
-     L.FLAG_DENOISE | L.FLAG_TEMPORAL_DENOISE | L.FLAG_AWB_HISTOGRAM,
-     dict(denoise_strength=1.0, denoise_temporal_strength=0.8), 3),
+    ("temporal_mhc_chroma", 390, 262, L.DEBAYER_MHC, L.CS_P3D65,
+     L.FLAG_DENOISE | L.FLAG_TEMPORAL_DENOISE | L.FLAG_CHROMA_DENOISE | L.FLAG_AWB_HISTOGRAM,
+     dict(denoise_strength=1.0, denoise_temporal_strength=0.8, denoise_chroma_strength=0.5), 3),
+    ("highlights_rcd", 704, 398, L.DEBAYER_RCD, L.CS_BT709,
+     L.FLAG_HIGHLIGHT_RECONSTRUCTION | L.FLAG_AWB_HISTOGRAM, dict(flags=L.FRAME_HIGHLIGHT_RECONSTRUCTION), 1),
     ("fp16_keep", 642, 386, L.DEBAYER_RCD, L.CS_BT2020, L.FLAG_AWB_HISTOGRAM | L.FLAG_KEEP_INTERMEDIATE,
      {}, 1),
 ]
@@ -52,7 +55,8 @@ def run_cases() -> dict[str, np.ndarray]:
             fp = L.frame_params(prof, noise_override=W.noise_model(4.0, 40.0), **kw)
             with L.Pipeline(ctx, pp) as pipe:
                 for f in range(nfr):
-                    m = W.synth_frame(w, h, 17 * w + h + f, noise_a_dn=4.0, noise_b_dn=40.0)
+                    m = (W.highlight_frame(w, h, 55 + f) if name.startswith("highlights") else
+                         W.synth_frame(w, h, 17 * w + h + f, noise_a_dn=4.0, noise_b_dn=40.0))
                     out[f"{name}/{f}"] = develop(pipe, m, fp)
                 out[f"{name}/hist"] = pipe.awb_histogram().count
                 out[f"{name}/errors"] = np.array([pipe.kernel_errors()], np.uint32)

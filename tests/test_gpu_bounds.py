@@ -1,6 +1,6 @@
 """GPU: the bounds-checked build (libcraw_bounds.so, every global index of
-the develop and denoise kernels checked against its buffer, a bad one
-recorded as CRAW_K_ERR_BOUNDS and skipped) develops the cases of
+the develop, denoise, chroma and highlight kernels checked against its
+buffer, a bad one recorded as CRAW_K_ERR_BOUNDS and skipped) develops the cases of
 bounds_cases.py in a process of its own with no error bit set, and
 gives the product build's outputs bit for bit."""
 import os
