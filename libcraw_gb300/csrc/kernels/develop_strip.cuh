@@ -3,9 +3,9 @@
  * lib/ref/ref_debayer.c:204-395; the passes of lib/shaders/rcd.comp.glsl).
  *
  * A CTA of SNT threads owns a strip of quad columns, one column a thread,
- * and walks down a segment of it one quad row (two pixel rows) a step. Each pass of the
- * RCD runs a fixed number of quad rows behind the one before it, so a step
- * does every pass once for every column:
+ * and walks down a segment of it one quad row (two pixel rows) a step.
+ * Each pass of the RCD runs a fixed number of quad rows behind the one
+ * before it, so a step does every pass once for every column:
  *
  *   stage A   D, L of quad row s (the four discriminations of the quad's
  *             pixels, the low pass at R and B);

@@ -383,9 +383,10 @@ CRAW_DEV void rq_green_site(float wt, float g00, float dh0, float dh1, float ev0
  * per 2x2 CFA quad (R at (0,0), Gr (1,0), Gb (0,1), B (1,1)): the site of
  * every value is static, the neighbours a quad's four sites share are
  * read once, and shared memory moves in float2 and float4. Same passes,
- * same formulas as the per-pixel version above; the only arithmetic
- * difference is the order of the 3x3 sums of the discriminations, taken
- * here as rows of three and then three rows.
+ * same formulas as the per-pixel version above, evaluated by the rq_*
+ * helpers with every rounding explicit (the strips evaluate them the same
+ * way), and the 3x3 sums of the discriminations taken as rows of three and
+ * then three rows.
  *
  * Arrays (tile-relative pixel or quad coordinates, their ranges):
  *   Vp float   pixels [-6, TW+6) x [-6, TH+6)   the prepped mosaic
