@@ -886,9 +886,9 @@ def run_target(ctx, stream, nframes: int = 24, plain_frames: int = 6, streams: i
     included. Frames/s of: the plain FP32 pipeline; the fused FP16 pipeline
     (device-resident frames, CUDA events); the frame server developing
     `streams` such clips at once from pinned host memory to pinned host
-    memory (saturated). The batch (one persistent launch for many frames)
-    takes spatial frames only, so it does not run this chain. And the fused
-    output's error against the FP64 oracle on a 256x128 window in the
+    memory, RGB32F out (saturated). The batch (one persistent launch for
+    many frames) takes spatial frames only, so it does not run this chain.
+    And the fused output's error against the FP64 oracle on a 256x128 window in the
     middle of a frame with a history (the oracle fed the state the GPU
     left: the crop of frame 1's mosaic developed from frame 0's state)."""
     import torch
@@ -934,9 +934,9 @@ def run_target(ctx, stream, nframes: int = 24, plain_frames: int = 6, streams: i
 
     # Served: `streams` clips at once, every frame submitted up front.
     pin_in = [torch.from_numpy(f.view(np.int16)).pin_memory() for f in host]
-    outs = [torch.empty((h, w, 4), dtype=torch.float32).pin_memory() for _ in range(2 * streams)]
+    outs = [torch.empty((h, w, 3), dtype=torch.float32).pin_memory() for _ in range(2 * streams)]
     pp16 = L.pipeline_params(w, h, debayer=L.DEBAYER_RCD, out_space=L.CS_ACES_AP1, flags=flags,
-                             out_format=L.FORMAT_RGBA32F, storage=L.STORAGE_FP16)
+                             out_format=L.FORMAT_RGB32F, storage=L.STORAGE_FP16)
     with L.Server(ctx, L.server_params(hbm_budget=60 << 30, max_inflight=2 * streams,
                                        slots_per_stream=2)) as srv:
         sids = [srv.open(L.server_stream_params(pp16)) for _ in range(streams)]
@@ -944,7 +944,7 @@ def run_target(ctx, stream, nframes: int = 24, plain_frames: int = 6, streams: i
         for i in range(nframes):
             for k, sid in enumerate(sids):
                 o = outs[(i % 2) * streams + k]
-                srv.submit(sid, pin_in[(i + k) % 4].data_ptr(), w * 2, o.data_ptr(), w * 16, fp, i / 24.0,
+                srv.submit(sid, pin_in[(i + k) % 4].data_ptr(), w * 2, o.data_ptr(), w * 12, fp, i / 24.0,
                            (k << 32) | i)
         srv.drain()
         wall = time.perf_counter() - t0
@@ -956,7 +956,7 @@ def run_target(ctx, stream, nframes: int = 24, plain_frames: int = 6, streams: i
             got += r
     res["served_fp16"] = {"streams": streams, "frames": len(got), "fps": len(got) / wall,
                           "device_ms_mean": float(np.mean([r.device_ms for r in got])),
-                          "how": "host to host: pinned mosaic in, pinned RGBA32F out, inside the timing"}
+                          "how": "host to host: pinned mosaic in, pinned RGB32F out, inside the timing"}
     base = res["plain_fp32_fps"]
     res["fused_fp16_vs_plain_fp32"] = res["fused_fp16_fps"] / base
     res["served_fp16_vs_plain_fp32"] = res["served_fp16"]["fps"] / base
@@ -1003,10 +1003,11 @@ def run_serve(ctx, seconds: float = 5.0, frames_per_clip: int = 120) -> dict:
     admitted under a 60 GB budget; clips run temporal 0.8 + NLM 1.0 + RCD +
     ACES AP0 float32 (stills the same without the temporal stage, each
     still being a new scene), from pinned host memory to pinned host
-    memory. Paced: frames are submitted at their arrival times for
-    `seconds` (at most frames_per_clip per clip); latency is submission to
-    the result in host memory. Saturated: every frame of the same schedule
-    submitted at once, for the aggregate throughput."""
+    memory, out as RGB32F (three floats a pixel). Paced: frames are
+    submitted at their arrival times for `seconds` (at most
+    frames_per_clip per clip); latency is submission to the result in host
+    memory. Saturated: every frame of the same schedule submitted at once,
+    for the aggregate throughput."""
     import torch
     import libcraw_gb300 as L
     from libcraw_gb300 import workloads as W
@@ -1022,13 +1023,13 @@ def run_serve(ctx, seconds: float = 5.0, frames_per_clip: int = 120) -> dict:
                                               noise_a_dn=a_dn, noise_b_dn=b_dn,
                                               movers=movers if clip else []).view(np.int16)).pin_memory()
                for i in range(4)]
-        dst = [torch.empty((h, w, 4), dtype=torch.float32).pin_memory() for _ in range(3)]
+        dst = [torch.empty((h, w, 3), dtype=torch.float32).pin_memory() for _ in range(3)]
         kw = dict(denoise_strength=1.0, noise_override=W.noise_model(a_dn, b_dn))
         if clip:
             kw["denoise_temporal_strength"] = 0.8
         flags = L.FLAG_DENOISE | (L.FLAG_TEMPORAL_DENOISE if clip else 0)
         pp = L.pipeline_params(w, h, debayer=L.DEBAYER_RCD, out_space=L.CS_ACES_AP0, flags=flags,
-                               out_format=L.FORMAT_RGBA32F)
+                               out_format=L.FORMAT_RGB32F)
         if clip:
             times = [i / rate for i in range(min(frames_per_clip, int(seconds * rate)))]
         else:
@@ -1064,7 +1065,7 @@ def run_serve(ctx, seconds: float = 5.0, frames_per_clip: int = 120) -> dict:
                 srcb, dstb = s["src"][i % 4], s["dst"][i % 3]
                 while True:
                     try:
-                        srv.submit(s["sid"], srcb.data_ptr(), s["w"] * 2, dstb.data_ptr(), s["w"] * 16,
+                        srv.submit(s["sid"], srcb.data_ptr(), s["w"] * 2, dstb.data_ptr(), s["w"] * 12,
                                    s["fp"], t, (k << 32) | i)
                         break
                     except L.CrawError as e:
@@ -1100,7 +1101,7 @@ def run_serve(ctx, seconds: float = 5.0, frames_per_clip: int = 120) -> dict:
     saturated = run(False)
     return {"workload": "8 streams: 2x1920x1080@60, 3x3840x2160@30, 2x5760x3240@24 (temporal 0.8 + "
                         "NLM 1.0 + RCD + ACES AP0 f32), 1x6000x4000 stills Poisson 2/s (NLM + RCD + "
-                        "AP0); pinned host in and out; 60 GB budget; clips' deadline = their frame "
+                        "AP0); pinned host in, pinned RGB32F out; 60 GB budget; clips' deadline = their frame "
                         "interval",
             "seconds": seconds, "paced": paced, "saturated": saturated,
             "p99_under_60fps_interval": paced["p99_ms"] < 1000.0 / 60}
