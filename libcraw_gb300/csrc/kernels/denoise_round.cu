@@ -48,6 +48,9 @@ constexpr int WIN = 9;                 /* search 3 + patch 1, both sides */
 constexpr int KW = 1;                  /* bit-map words a lane scans a step */
 constexpr int GA = 4;                  /* lanes of the decision stage a sample */
 constexpr int G = 16;                  /* lanes of the exact stage a sample */
+constexpr int GPL = (WIN * WIN + GA - 1) / GA;   /* window samples a decision lane loads */
+constexpr int XPL = (WIN * WIN + G - 1) / G;     /* and an exact-stage lane */
+constexpr int DECIDE_CTAS = 7;         /* resident decision CTAs an SM (72 registers) */
 constexpr float U = 0x1p-24f;          /* float unit roundoff */
 
 /* ------------------------------------------------------------ helpers */
@@ -121,17 +124,33 @@ CRAW_DEV bool decide(const CRAWKDenoise &k, const CRAWKDenoiseExact &e, const CR
     const float mc = stab(e, pl, (uint32_t)code);
     const float q = e.q[pl];
     if (ok) {
+        /* The lane's window samples, every GA-th: all loads issued before
+         * any is used, so that their latencies overlap. */
         const bool inner = qy >= 4 && qy + 4 < k.ph && qx >= 4 && qx + 4 < k.pw;
-        for (int s = g; s < WIN * WIN; s += GA) {
-            int yy = qy + s / WIN - 4, xx = qx + s % WIN - 4;
-            if (!inner) {
-                yy = craw_mirror(yy, k.ph);
-                xx = craw_mirror(xx, k.pw);
+        uint32_t raw[(GPL + 1) / 2];        /* two codes a register */
+#pragma unroll
+        for (int i = 0; i < GPL; i++) {
+            const int s = g + i * GA;
+            uint32_t r = 0u;
+            if (s < WIN * WIN) {
+                int yy = qy + s / WIN - 4, xx = qx + s % WIN - 4;
+                if (!inner) {
+                    yy = craw_mirror(yy, k.ph);
+                    xx = craw_mirror(xx, k.pw);
+                }
+                r = __ldg(row16(io.src, io.src_pitch, 2 * yy + py) + 2 * xx + px);
             }
-            const uint32_t r = row16(io.src, io.src_pitch, 2 * yy + py)[2 * xx + px];
-            if (r <= e.dark_code)
-                ok = false;                 /* a sample at or below black: exact stage */
-            D[s] = (float)((int)r - code) * q * __frcp_rn(stab(e, pl, r) + mc);
+            raw[i >> 1] = (i & 1) ? raw[i >> 1] | (r << 16) : r;
+        }
+#pragma unroll
+        for (int i = 0; i < GPL; i++) {
+            const int s = g + i * GA;
+            const uint32_t r = (raw[i >> 1] >> (16 * (i & 1))) & 0xffffu;
+            if (s < WIN * WIN) {
+                if (r <= e.dark_code)
+                    ok = false;             /* a sample at or below black: exact stage */
+                D[s] = (float)((int)r - code) * q * __frcp_rn(stab(e, pl, r) + mc);
+            }
         }
     }
     /* The group goes on only if all its lanes may. */
@@ -304,13 +323,21 @@ CRAW_DEV void decide_batch(const CRAWKDenoise &k, const CRAWKDenoiseExact &e, co
                            uint32_t *list, uint32_t list_cap, uint32_t *stats)
 {
     const bool valid = lane / GA < take;
-    if (lane == 0)
-        atomicAdd(&stats[0], (uint32_t)take);
     const uint32_t qx = v % (uint32_t)k.pw, r = v / (uint32_t)k.pw;
     const int qy = (int)(r % (uint32_t)k.ph), pl = (int)(r / (uint32_t)k.ph);
     const bool done = decide(k, e, io, pl, (int)qx, qy, valid, g, lane, D, stats);
-    if (valid && !done && g == 0) {
-        const uint32_t slot = atomicAdd(rd.count2, 1u);
+    /* The batch's undecided samples take their places in the list with
+     * one atomic. */
+    const bool put = valid && !done && g == 0;
+    const uint32_t bal = __ballot_sync(0xffffffffu, put);
+    if (!bal)
+        return;
+    uint32_t base = 0;
+    if (lane == 0)
+        base = atomicAdd(rd.count2, (uint32_t)__popc(bal));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (put) {
+        const uint32_t slot = base + (uint32_t)__popc(bal & ((1u << lane) - 1u));
         if (slot < list_cap)
             list[slot] = v;
     }
@@ -324,7 +351,7 @@ CRAW_DEV void decide_batch(const CRAWKDenoise &k, const CRAWKDenoiseExact &e, co
  * image is bright, so fixed shares would leave a few warps with most of
  * the work) and queue each step's marked samples, so that every batch but
  * a warp's last fills all its groups. */
-__global__ void __launch_bounds__(NT)
+__global__ void __launch_bounds__(NT, DECIDE_CTAS)
 k_round_decide(const CRAWKDenoise k, const CRAWKDenoiseExact e, const CRAWKDenoiseIO io, const CRAWKRound rd,
                const uint32_t *marked, uint32_t marked_cap, uint32_t *list, uint32_t list_cap,
                uint32_t *stats)
@@ -335,6 +362,8 @@ k_round_decide(const CRAWKDenoise k, const CRAWKDenoiseExact e, const CRAWKDenoi
     float *D = Dw[threadIdx.x / GA];
     const uint32_t nm = *(volatile const uint32_t *)(rd.count2 + 2);
     if (nm <= marked_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            atomicAdd(&stats[0], nm);
         const long long warps = (long long)gridDim.x * (NT / 32);
         const long long wid = (long long)blockIdx.x * (NT / 32) + threadIdx.x / 32;
         for (long long b = wid * BATCH; b < nm; b += warps * BATCH) {
@@ -348,6 +377,7 @@ k_round_decide(const CRAWKDenoise k, const CRAWKDenoiseExact e, const CRAWKDenoi
     const int ww = CRAW_K_ROUND_WW(k.pw);
     const long long nwords = (long long)CRAW_K_ROUND_WORDS(k.pw, k.ph);
     int qn = 0;               /* the same on every lane, as is `more` */
+    uint32_t taken = 0;
     bool more = true;
     while (more || qn > 0) {
         if (more) {
@@ -365,9 +395,12 @@ k_round_decide(const CRAWKDenoise k, const CRAWKDenoiseExact e, const CRAWKDenoi
             const uint32_t v = lane / GA < take ? Q[qn - take + lane / GA] : 0u;
             __syncwarp();   /* read before the next steps write over it */
             qn -= take;
+            taken += (uint32_t)take;
             decide_batch(k, e, io, rd, v, take, g, lane, D, list, list_cap, stats);
         }
     }
+    if (lane == 0 && taken)
+        atomicAdd(&stats[0], taken);
 }
 
 /* ------------------------------------------------ the double-float stage */
@@ -412,11 +445,25 @@ CRAW_DEV void exact_sample(const CRAWKDenoiseExact &e, const CRAWKDenoiseIO &io,
 {
     const int px = pl & 1, py = pl >> 1;
     if (valid) {
-        for (int s = g; s < WIN * WIN; s += G) {
-            const int yy = craw_mirror(qy + s / WIN - 4, e.ph), xx = craw_mirror(qx + s % WIN - 4, e.pw);
-            const dfl t = gat_fwd_x(e, row16(io.src, io.src_pitch, 2 * yy + py)[2 * xx + px], pl);
-            Th[s] = t.hi;
-            Tl[s] = t.lo;
+        /* Every G-th window sample, the loads issued first. */
+        uint32_t raw[XPL];
+#pragma unroll
+        for (int i = 0; i < XPL; i++) {
+            const int s = g + i * G;
+            raw[i] = 0u;
+            if (s < WIN * WIN) {
+                const int yy = craw_mirror(qy + s / WIN - 4, e.ph), xx = craw_mirror(qx + s % WIN - 4, e.pw);
+                raw[i] = __ldg(row16(io.src, io.src_pitch, 2 * yy + py) + 2 * xx + px);
+            }
+        }
+#pragma unroll
+        for (int i = 0; i < XPL; i++) {
+            const int s = g + i * G;
+            if (s < WIN * WIN) {
+                const dfl t = gat_fwd_x(e, raw[i], pl);
+                Th[s] = t.hi;
+                Tl[s] = t.lo;
+            }
         }
     }
     __syncwarp();
@@ -511,7 +558,7 @@ extern "C" int craw_k_denoise_round(const CRAWKDenoise *k, const CRAWKDenoiseExa
     k_round_compact<<<(unsigned)(ctas_c > 0 ? ctas_c : 1), NT, 0, s>>>(*rd, k->pw, k->ph, marked, (uint32_t)cap);
     if (cudaGetLastError() != cudaSuccess)
         return -5;
-    k_round_decide<<<(unsigned)sms * 8, NT, 0, s>>>(*k, *e, *io, *rd, marked, (uint32_t)cap, undecided,
+    k_round_decide<<<(unsigned)sms * DECIDE_CTAS, NT, 0, s>>>(*k, *e, *io, *rd, marked, (uint32_t)cap, undecided,
                                                     (uint32_t)cap, stats);
     if (cudaGetLastError() != cudaSuccess)
         return -5;
