@@ -166,11 +166,20 @@ CRAW_API int craw_awb_smoother_push(CRAWAwbSmoother *sm, double pts_s,
  *    with CRAW_ERROR(EINVAL) and a log line, before any device work;
  *  - the first call on each device does the set-up: it looks up the device
  *    address of the scratch array (cudaGetSymbolAddress, with that device
- *    current) and keeps it for the process (a failed lookup is retried on
- *    the next call). Make that first call before any stream capture
- *    begins. A cudaDeviceReset() (or any other teardown of the device's
- *    primary context) leaves the kept address stale: do not call this
- *    entry point on a device after resetting it;
+ *    current) and registers a 200 KB host staging area with
+ *    cudaHostRegister, and keeps both for the process (a failed set-up is
+ *    retried on the next call). Make that first call before any stream
+ *    capture begins. A cudaDeviceReset() (or any other teardown of the
+ *    device's primary context) leaves the kept address stale: do not call
+ *    this entry point on a device after resetting it;
+ *  - after the set-up a call makes only asynchronous copies (into the
+ *    staging area) and waits on `stream` alone, with the calling thread's
+ *    capture interaction relaxed for the call
+ *    (cudaThreadExchangeStreamCaptureMode, restored before it returns).
+ *    So it may run while another thread holds a global-mode stream
+ *    capture, given a `stream` created with cudaStreamNonBlocking that is
+ *    not itself capturing (the legacy default stream would synchronise
+ *    with the capturing one);
  *  - a CUDA error that an earlier call left pending on the calling thread
  *    is reported (CRAW_ERROR(EIO)), not cleared;
  *  - the histograms and the counter in the scratch must be zero when the

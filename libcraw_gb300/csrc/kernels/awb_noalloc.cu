@@ -15,6 +15,8 @@
 #include <math.h>
 #include <stddef.h>
 #include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
 
 #include <mutex>
 
@@ -115,14 +117,25 @@ k_awb_noalloc(const float *rgb, int w, int h, size_t stride, int ch, float wb0, 
     atomicAdd(&sc[2 * kBins2 + bin], bq);
 }
 
-/* The scratch's device address, looked up on the first call on each
- * device (cudaGetSymbolAddress with that device current) and kept; a
- * lookup that fails is not kept, so the next call tries again. */
+/* The host side of a call's copies: the histograms and the counter, then
+ * the deferred blocks a chunk at a time, through one page-locked area per
+ * device. Copies into page-locked memory are asynchronous, so the call
+ * makes none of the implicitly synchronising copies (pageable host
+ * memory) that another thread's global-mode stream capture forbids. */
+constexpr uint32_t kChunk = 1024;                       /* deferred blocks a copy */
+constexpr size_t kStageWords = kCounter + 1 > 3 * kChunk ? kCounter + 1 : 3 * kChunk;
+constexpr size_t kStageBytes = (kStageWords * sizeof(uint32_t) + 4095) & ~(size_t)4095;
+
+/* Set up on the first call on each device and kept: the scratch's device
+ * address (cudaGetSymbolAddress with that device current) and the staging
+ * area (host memory registered with cudaHostRegister). A set-up that fails
+ * keeps nothing, so the next call tries again. */
 constexpr int kMaxDevices = 64;
 std::mutex setup_lock;
 uint32_t *setup_ptr[kMaxDevices];
+uint32_t *stage_ptr[kMaxDevices];
 
-int scratch_address(uint32_t **out)
+int setup(uint32_t **sc, uint32_t **stage)
 {
     int dev = -1;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
@@ -139,7 +152,73 @@ int scratch_address(uint32_t **out)
         }
         setup_ptr[dev] = static_cast<uint32_t *>(p);
     }
-    *out = setup_ptr[dev];
+    if (!stage_ptr[dev]) {
+        void *h = aligned_alloc(4096, kStageBytes);
+        if (!h)
+            return CRAW_ERROR(ENOMEM);
+        const cudaError_t err = cudaHostRegister(h, kStageBytes, cudaHostRegisterDefault);
+        if (err != cudaSuccess) {
+            (void)cudaGetLastError();   /* this registration's own error */
+            free(h);
+            craw_log(NULL, CRAW_LOG_ERROR, "craw_awb_histogram_from_rgb_cuda_noalloc: "
+                     "cudaHostRegister failed on device %d: %s\n", dev, cudaGetErrorString(err));
+            return CRAW_ERROR(EIO);
+        }
+        stage_ptr[dev] = static_cast<uint32_t *>(h);
+    }
+    *sc = setup_ptr[dev];
+    *stage = stage_ptr[dev];
+    return 0;
+}
+
+/* A failed CUDA call of this entry point: logged with its error, which is
+ * read (and so cleared) because it is the call's own; EIO. */
+int cuda_failed(const char *what)
+{
+    const cudaError_t err = cudaGetLastError();
+    craw_log(NULL, CRAW_LOG_ERROR, "craw_awb_histogram_from_rgb_cuda_noalloc: %s failed: %s\n", what,
+             cudaGetErrorString(err));
+    return CRAW_ERROR(EIO);
+}
+
+/* The device work and the copies of one call, once the scratch and the
+ * staging area are set up. */
+int histogram(const float *rgb, uint32_t width, uint32_t height, size_t stride, int channels,
+              const float wb_applied[3], uint32_t *count, uint32_t *weight, uint32_t *weight_bright,
+              cudaStream_t stream, uint32_t *sc, uint32_t *stage)
+{
+    if (cudaMemsetAsync(sc, 0, (kCounter + 1) * sizeof(uint32_t), stream) != cudaSuccess)
+        return cuda_failed("cudaMemsetAsync");
+    if (width && height) {
+        const dim3 grid((unsigned)(((width + 7) / 8 + 31) / 32), (unsigned)(((height + 7) / 8 + 7) / 8));
+        k_awb_noalloc<<<grid, 256, 0, stream>>>(rgb, (int)width, (int)height, stride, channels,
+                                                 wb_applied[0], wb_applied[2], sc);
+        if (cudaGetLastError() != cudaSuccess)
+            return cuda_failed("the kernel launch");
+    }
+    /* The three histograms and the counter lie together: one copy. */
+    if (cudaMemcpyAsync(stage, sc, (kCounter + 1) * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                        stream) != cudaSuccess)
+        return cuda_failed("cudaMemcpyAsync");
+    if (cudaStreamSynchronize(stream) != cudaSuccess)
+        return cuda_failed("cudaStreamSynchronize");
+    memcpy(count, stage, kBins2 * sizeof(uint32_t));
+    memcpy(weight, stage + kBins2, kBins2 * sizeof(uint32_t));
+    memcpy(weight_bright, stage + 2 * kBins2, kBins2 * sizeof(uint32_t));
+    const uint32_t nd = stage[kCounter];
+    /* Bin the deferred blocks with this host's logf, a chunk at a time. */
+    for (uint32_t i = 0; i < nd;) {
+        const uint32_t k = nd - i < kChunk ? nd - i : kChunk;
+        if (cudaMemcpyAsync(stage, sc + kDeferred + 3 * i, 3 * k * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                            stream) != cudaSuccess)
+            return cuda_failed("cudaMemcpyAsync");
+        if (cudaStreamSynchronize(stream) != cudaSuccess)
+            return cuda_failed("cudaStreamSynchronize");
+        const float *d = reinterpret_cast<const float *>(stage);
+        for (uint32_t j = 0; j < k; j++)
+            craw_awb_bin_host(d[3 * j], d[3 * j + 1], d[3 * j + 2], count, weight, weight_bright);
+        i += k;
+    }
     return 0;
 }
 
@@ -151,8 +230,7 @@ extern "C" CRAW_API int craw_awb_histogram_from_rgb_cuda_noalloc(
     cudaStream_t stream)
 {
     const uint64_t blocks = (((uint64_t)width + 7) / 8) * (((uint64_t)height + 7) / 8);
-    uint32_t *sc = nullptr;
-    uint32_t nd = 0;
+    uint32_t *sc = nullptr, *stage = nullptr;
     int ret;
 
     if (!rgb || !wb_applied || !count || !weight || !weight_bright)
@@ -173,37 +251,19 @@ extern "C" CRAW_API int craw_awb_histogram_from_rgb_cuda_noalloc(
                  "earlier call is pending (%s)\n", cudaGetErrorString(cudaPeekAtLastError()));
         return CRAW_ERROR(EIO);
     }
-    if ((ret = scratch_address(&sc)) < 0)
+    if ((ret = setup(&sc, &stage)) < 0)
         return ret;
-    if (cudaMemsetAsync(sc, 0, (kCounter + 1) * sizeof(uint32_t), stream) != cudaSuccess)
-        return CRAW_ERROR(EIO);
-    if (blocks) {
-        const dim3 grid((unsigned)(((width + 7) / 8 + 31) / 32), (unsigned)(((height + 7) / 8 + 7) / 8));
-        k_awb_noalloc<<<grid, 256, 0, stream>>>(rgb, (int)width, (int)height, stride, channels,
-                                                 wb_applied[0], wb_applied[2], sc);
-        if (cudaGetLastError() != cudaSuccess)
-            return CRAW_ERROR(EIO);
-    }
-    if (cudaMemcpyAsync(count, sc, kBins2 * sizeof(uint32_t), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
-        cudaMemcpyAsync(weight, sc + kBins2, kBins2 * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                        stream) != cudaSuccess ||
-        cudaMemcpyAsync(weight_bright, sc + 2 * kBins2, kBins2 * sizeof(uint32_t),
-                        cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
-        cudaMemcpyAsync(&nd, sc + kCounter, sizeof(nd), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
-        cudaStreamSynchronize(stream) != cudaSuccess)
-        return CRAW_ERROR(EIO);
-    /* Bin the deferred blocks with this host's logf, a chunk at a time
-     * through a buffer on the stack. */
-    for (uint32_t i = 0; i < nd;) {
-        float d[1024][3];
-        const uint32_t k = nd - i < 1024 ? nd - i : 1024;
-        if (cudaMemcpyAsync(d, sc + kDeferred + 3 * i, k * sizeof(d[0]), cudaMemcpyDeviceToHost,
-                            stream) != cudaSuccess ||
-            cudaStreamSynchronize(stream) != cudaSuccess)
-            return CRAW_ERROR(EIO);
-        for (uint32_t j = 0; j < k; j++)
-            craw_awb_bin_host(d[j][0], d[j][1], d[j][2], count, weight, weight_bright);
-        i += k;
-    }
-    return 0;
+    /* The rest touches only `stream`, the scratch and the staging area, so
+     * it runs with this thread's capture interaction relaxed: a global-mode
+     * capture on another thread would otherwise refuse the wait on
+     * `stream`, which cannot touch a capturing stream unless it is one. The
+     * thread's own mode is restored before returning. */
+    cudaStreamCaptureMode mode = cudaStreamCaptureModeRelaxed;
+    if (cudaThreadExchangeStreamCaptureMode(&mode) != cudaSuccess)
+        return cuda_failed("cudaThreadExchangeStreamCaptureMode");
+    ret = histogram(rgb, width, height, stride, channels, wb_applied, count, weight, weight_bright, stream, sc,
+                    stage);
+    if (cudaThreadExchangeStreamCaptureMode(&mode) != cudaSuccess && ret == 0)
+        ret = cuda_failed("cudaThreadExchangeStreamCaptureMode");
+    return ret;
 }

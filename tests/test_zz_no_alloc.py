@@ -99,3 +99,58 @@ def test_noalloc_rejects_beyond_scratch():
     assert int(ref[0].sum()) == limit
     for g_, r_ in zip(got, ref):
         assert np.array_equal(g_, r_)
+
+
+def test_noalloc_while_another_thread_captures():
+    """After its set-up call on the device, the entry point runs while
+    another thread holds a global-mode stream capture (the case it exists
+    for: the caller cannot allocate then). The call returns 0 with the CPU
+    builder's histograms, and the other thread's capture still ends and
+    its graph replays."""
+    import threading
+
+    w, h, ch = 256, 160, 4
+    img, wb = rgb_image(w, h, ch, 7)
+    dev = torch.from_numpy(img).cuda()
+    stream = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    ret, _ = gpu_hist(dev, w, h, w * ch, ch, wb, stream.cuda_stream)   # the set-up call
+    assert ret == 0
+    x = torch.arange(1024, dtype=torch.float32, device="cuda")
+    y = torch.zeros_like(x)
+    cap_stream = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+    torch.cuda.synchronize()
+    started, release = threading.Event(), threading.Event()
+    errors = []
+
+    def capture():
+        try:
+            torch.cuda.set_device(dev.device)
+            with torch.cuda.stream(cap_stream):
+                graph.capture_begin(capture_error_mode="global")
+                try:
+                    torch.mul(x, 2.0, out=y)
+                    started.set()
+                    release.wait(30)
+                finally:
+                    graph.capture_end()
+        except Exception as e:   # reported by the main thread
+            errors.append(e)
+            started.set()
+
+    t = threading.Thread(target=capture)
+    t.start()
+    try:
+        assert started.wait(30)
+        ret, got = gpu_hist(dev, w, h, w * ch, ch, wb, stream.cuda_stream)
+    finally:
+        release.set()
+        t.join(60)
+    assert ret == 0 and not errors, (ret, errors)
+    ref = cpu_hist(img, wb)
+    for name, g, r in zip(("count", "weight", "weight_bright"), got, ref):
+        assert np.array_equal(g, r), name
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(y, x * 2.0)
