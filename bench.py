@@ -79,6 +79,9 @@ def parse():
                          "highlights, noise, cpu")
     ap.add_argument("--force-shape", type=int, default=-1,
                     help="denoise tile shape index instead of the autotuner's (profiling)")
+    ap.add_argument("--rcd", default="auto", choices=["auto", "tiles", "strips"],
+                    help="RCD interior by 64x16 tiles or by strips instead of the library's choice "
+                         "(profiling)")
     ap.add_argument("--e2e-lanes", type=int, default=0,
                     help="pipelines the end-to-end leg rotates over (0: the default)")
     ap.add_argument("--width", type=int, default=None, help="frame width (default: the workload's)")
@@ -371,6 +374,9 @@ def run_gpu(args):
     if args.force_shape >= 0:
         # A fixed denoise shape and no autotuner launches, for profiling runs.
         L.debug_force_denoise_shape(args.force_shape)
+    if args.rcd != "auto":
+        # The RCD interior by tiles or by strips whatever the colour stage.
+        L.debug_rcd_strips(0 if args.rcd == "tiles" else 2)
     stream = torch.cuda.Stream()
     sptr = stream.cuda_stream
 
