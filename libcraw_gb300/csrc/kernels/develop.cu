@@ -68,10 +68,20 @@ struct QuadGrid {
     }
 };
 
+/* An interior kernel lets the border launch that follows it on the stream
+ * begin at once (programmatic dependent launch): the two write disjoint
+ * tiles, and the border CTAs take the SM slots that the interior's last
+ * wave leaves idle. The launches after the border wait for both as usual. */
+CRAW_DEV void release_border()
+{
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __global__ void __launch_bounds__(QNT)
 k_develop_rcd_quads(const CRAWKDevelop k, const CRAWKDevelopIO io, const QuadGrid g)
 {
     extern __shared__ __align__(16) float smem[];
+    release_border();
     rcd_quad_tile(k, io, (g.c_lo + blockIdx.x) * QTW, (g.r_lo + blockIdx.y) * QTH, smem);
 }
 
@@ -91,6 +101,7 @@ k_develop_rcd_quads_tma(const CRAWKDevelop k, const CRAWKDevelopIO io, const Qua
 {
     extern __shared__ __align__(16) float smem[];
     __shared__ __align__(8) uint64_t bar_s;
+    release_border();
     const int x0 = (g.c_lo + blockIdx.x) * QTW, y0 = (g.r_lo + blockIdx.y) * QTH;
     RcdQuads<QTW, QTH, QNT> t;
     t.carve(smem);
@@ -121,6 +132,7 @@ __global__ void __launch_bounds__(SNT, 4)
 k_develop_rcd_strips(const CRAWKDevelop k, const CRAWKDevelopIO io, const StripGrid g)
 {
     extern __shared__ __align__(16) float smem[];
+    release_border();
     rcd_strip(k, io, g, blockIdx.x, blockIdx.y, *reinterpret_cast<StripSmem *>(smem));
 }
 
@@ -231,8 +243,19 @@ int launch_rcd(const CRAWKDevelop *k, const CRAWKDevelopIO *io, cudaStream_t s)
             return -5;
     }
     if (g.border_quads() > 0) {
-        k_develop_rcd_border<<<g.border_quads() * (QTW / BTW), 256,
-                               PixelSmem<kRcd, BTW, BTH, 256>::floats * sizeof(float), s>>>(*k, *io, g);
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)(g.border_quads() * (QTW / BTW)));
+        cfg.blockDim = dim3(256);
+        cfg.dynamicSmemBytes = PixelSmem<kRcd, BTW, BTH, 256>::floats * sizeof(float);
+        cfg.stream = s;
+        cudaLaunchAttribute early[1];
+        early[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        early[0].val.programmaticStreamSerializationAllowed = 1;
+        /* After an interior launch only: it is the launch the border may
+         * overlap. */
+        cfg.attrs = early;
+        cfg.numAttrs = g.interior_x() > 0 && g.interior_y() > 0 ? 1 : 0;
+        (void)cudaLaunchKernelEx(&cfg, k_develop_rcd_border, *k, *io, g);
         if (cudaGetLastError() != cudaSuccess)
             return -5;
     }
