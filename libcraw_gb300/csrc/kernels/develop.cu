@@ -255,7 +255,13 @@ int launch_rcd(const CRAWKDevelop *k, const CRAWKDevelopIO *io, cudaStream_t s)
          * overlap. */
         cfg.attrs = early;
         cfg.numAttrs = g.interior_x() > 0 && g.interior_y() > 0 ? 1 : 0;
-        (void)cudaLaunchKernelEx(&cfg, k_develop_rcd_border, *k, *io, g);
+        if (cudaLaunchKernelEx(&cfg, k_develop_rcd_border, *k, *io, g) != cudaSuccess && cfg.numAttrs) {
+            /* A driver that refuses the early start: the plain launch
+             * after the interior, the launch's own error cleared. */
+            (void)cudaGetLastError();
+            cfg.numAttrs = 0;
+            (void)cudaLaunchKernelEx(&cfg, k_develop_rcd_border, *k, *io, g);
+        }
         if (cudaGetLastError() != cudaSuccess)
             return -5;
     }
