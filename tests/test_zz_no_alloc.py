@@ -1,9 +1,11 @@
 """GPU: craw_awb_histogram_from_rgb_cuda_noalloc, the AWB histogram of a
 device RGB image built in a fixed static scratch with no allocation, against
 craw_awb_histogram_from_rgb (the CPU builder) on the same image: the three
-histograms must be equal bit for bit, on two calls in a row. The file is
-named to be collected last, so that it also runs after every other GPU test
-in the same process; it passes alone as well."""
+histograms must be equal bit for bit, on two calls in a row, and while
+another thread holds a global-mode stream capture (whose graph must still
+capture and replay). The file is named to be collected last, so that it
+also runs after every other GPU test in the same process; it passes alone
+as well."""
 import ctypes as C
 import errno
 
